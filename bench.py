@@ -1,0 +1,476 @@
+#!/usr/bin/env python
+"""Benchmark of the BCn block encoder on one GB300 (or N replicas).
+
+Headline workload (one "step"): BC3 ClusterFit, default Params (perceptual
+weights, no alpha weighting) over one 2048x2048 RGBA8 texture (262,144
+blocks) whose colour is a per-block noisy two-endpoint ramp (10% flat
+blocks) and whose alpha is a per-block ramp with +-12 noise and 0/255
+extremes in 15% of blocks.  Seeded synthetic data: the reference publishes
+no benchmark inputs.
+
+  value   Mblocks/s of the kernel with inputs resident in HBM: K steps
+          replayed from one CUDA graph, each step on a different copy of the
+          texture (copies total > 3x L2), CUDA events on the launch stream.
+  e2e     the same metric through the drop-in C-ABI call tx_compress with
+          pinned host buffers: host->device copy of the RGBA8 input, kernel,
+          device->host copy of the blocks, every step.
+  roofline  FP32-issue roofline of the ClusterFit kernel (algorithmic FP32
+          operations = reference candidate evaluations x ops per candidate)
+          plus the HBM roofline of the same launch (80 B per block).
+  cpu_baseline  the CPU oracle (a C restatement of the reference's block
+          path) on all host cores, one block row per task as rayon does.
+  extra   the other formats / algorithms of the benchmark configurations,
+          each beside its CPU-oracle rate.
+
+`--impl reference` times the reference's CPU algorithm (the oracle; the Rust
+crate cannot be built without cargo) on the same workload and metric.
+
+Under torchrun with N processes every rank compresses its own replica
+(weak scaling, no data-path collective); value = all blocks / max time.
+"""
+import argparse
+import json
+import os
+import signal
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "Mblocks/s per format+algorithm vs host CPU"
+UNIT = "Mblocks/s"
+L2_BYTES = 129 * 1000 * 1000
+# FP32 operations of one candidate as the reference's body needs them
+# (x, y, z lanes of the endpoints, w lane of the sums; reciprocal counted once):
+# cluster.rs:320-353 (compress4) and :189-220 (compress3).
+OPS_CAND4 = 155
+OPS_CAND3 = 129
+BYTES_PER_BLOCK = {0: 72, 1: 80, 2: 80, 3: 72, 4: 80}          # RGBA8 in + block out
+BYTES_PER_BLOCK_NATIVE = {3: 24, 4: 48}                           # R8 / RG8 in + block out
+FMT = {"BC1": 0, "BC2": 1, "BC3": 2, "BC4": 3, "BC5": 4}
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=400)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--no-extra", action="store_true", help="skip the per-format extra lines")
+    ap.add_argument("--size", type=int, default=2048)
+    ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
+    return ap.parse_args()
+
+
+def n4(n):
+    return sum(n + 1 - max(j, 1) for i in range(n) for j in range(i, n + 1)) if n >= 2 else 0
+
+
+def n3(n):
+    return sum(n + 1 - max(i, 1) for i in range(n)) if n >= 2 else 0
+
+
+def distinct_colours(img, fmt):
+    """Distinct colours per block as the ColourSet counts them (colourset.rs:35-104)."""
+    from texpresso_gb300 import workloads
+    blocks, masks = workloads.image_to_blocks(img)
+    px = blocks.reshape(-1, 16, 4).astype(np.uint32)
+    key = px[..., 0] | (px[..., 1] << 8) | (px[..., 2] << 16)
+    valid = ((masks[:, None] >> np.arange(16, dtype=np.uint32)) & 1).astype(bool)
+    if fmt == 0:
+        valid &= px[..., 3] >= 128
+    key = np.where(valid, key, np.uint32(0xFF000000) + np.arange(16, dtype=np.uint32))
+    s = np.sort(key, axis=1)
+    uniq = 1 + (s[:, 1:] != s[:, :-1]).sum(axis=1)
+    invalid = (~valid).sum(axis=1)
+    transparent = (fmt == 0) & (((px[..., 3] < 128) & ((masks[:, None] >> np.arange(16)) & 1).astype(bool)).any(axis=1))
+    return uniq - invalid, transparent
+
+
+def cluster_ops(img, fmt):
+    """Algorithmic FP32 ops of one non-iterative ClusterFit launch over img."""
+    counts, transparent = distinct_colours(img, fmt)
+    t4 = np.array([n4(n) for n in range(17)], np.int64)
+    t3 = np.array([n3(n) for n in range(17)], np.int64)
+    c4 = t4[counts]
+    if fmt == 0:
+        c4 = np.where(transparent, 0, c4)
+        return int((t3[counts] * OPS_CAND3).sum() + (c4 * OPS_CAND4).sum())
+    return int((c4 * OPS_CAND4).sum())
+
+
+class Clocks:
+    """nvidia-smi sampler (clocks + throttle reasons) around a timed region."""
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap,utilization.gpu")
+
+    def __init__(self, gpu_index):
+        self.idx = gpu_index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.idx), "--query-gpu=" + self.FIELDS, "--format=csv,noheader,nounits",
+                 "-lms", "100"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.send_signal(signal.SIGTERM)
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 10:
+                continue
+            try:
+                rows.append((float(f[1]), float(f[2]), float(f[3]), f[5], f[6], f[7], f[8], float(f[9])))
+            except ValueError:
+                continue
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        load = [r for r in rows if r[7] > 0] or rows
+        reasons = set()
+        for r in load:
+            for name, v in zip(("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"), r[3:7]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(r[0] for r in load), "sm_max_mhz": max(r[1] for r in rows),
+                "power_w_max": max(r[2] for r in rows), "samples": len(rows), "samples_under_load": len(load),
+                "reasons": sorted(reasons)}
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), float(p.get("sm_max_mhz", 2070.0)), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, 2070.0, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# device timing
+
+class DeviceRun:
+    """K compressions replayed from one CUDA graph over rotating HBM copies."""
+
+    def __init__(self, torch, tx, fmt, imgs, params, channels=4):
+        self.torch, self.tx, self.fmt, self.params, self.ch = torch, tx, tx.Format(fmt), params, channels
+        h, w = imgs[0].shape[:2]
+        self.w, self.h = w, h
+        self.nblocks = tx.num_blocks(w) * tx.num_blocks(h)
+        self.out_len = self.fmt.compressed_size(w, h)
+        per = imgs[0].nbytes
+        copies = max(2, -(-3 * L2_BYTES // per))
+        self.src = [torch.from_numpy(np.ascontiguousarray(imgs[i % len(imgs)])).cuda() for i in range(copies)]
+        self.dst = [torch.empty(self.out_len, dtype=torch.uint8, device="cuda") for _ in range(copies)]
+        self.stream = torch.cuda.Stream()
+
+    def launch(self, i):
+        s = self.src[i % len(self.src)]
+        self.tx.compress_device(self.fmt, s.data_ptr(), self.w * self.ch, self.ch, self.w, self.h, self.params,
+                                self.dst[i % len(self.dst)].data_ptr(), self.out_len, self.stream.cuda_stream)
+
+    def time(self, steps, warmup):
+        torch = self.torch
+        with torch.cuda.stream(self.stream):
+            for i in range(warmup):
+                self.launch(i)
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        n0 = self.tx.kernel_launch_count()
+        with torch.cuda.graph(g, stream=self.stream):
+            for i in range(steps):
+                self.launch(i)
+        launches = self.tx.kernel_launch_count() - n0
+        torch.cuda.synchronize()
+        g.replay()  # warm the graph once
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(self.stream):
+            e0.record(self.stream)
+            g.replay()
+            e1.record(self.stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1), launches
+
+    def output(self, i=0):
+        return self.dst[i].cpu().numpy()
+
+
+def e2e_time(torch, tx, fmt, img, params, steps, warmup):
+    """tx_compress (host buffers, synchronous) on pinned memory, wall clock."""
+    h, w = img.shape[:2]
+    f = tx.Format(fmt)
+    src = torch.from_numpy(np.ascontiguousarray(img)).pin_memory()
+    dst = torch.empty(f.compressed_size(w, h), dtype=torch.uint8).pin_memory()
+    srcn, dstn = src.numpy(), dst.numpy()
+    for _ in range(warmup):
+        f.compress(srcn, w, h, params, dstn)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        f.compress(srcn, w, h, params, dstn)
+    dt = time.perf_counter() - t0
+    return dt * 1e3, src.numel(), dst.numel()
+
+
+# ---------------------------------------------------------------------------
+# CPU (oracle) timing
+
+def cpu_rate(oracle, fmt, img, params, seconds, nthreads=0):
+    """Mblocks/s of the oracle over repeated passes (or bands) for ~seconds."""
+    h, w = img.shape[:2]
+    bw = (w + 3) // 4
+    rows_total = (h + 3) // 4
+    # calibrate on a band of 1/16 of the rows
+    band = max(1, rows_total // 16)
+    t0 = time.perf_counter()
+    oracle.compress(fmt, img[:4 * band], w, 4 * band, params, nthreads=nthreads)
+    per_row = (time.perf_counter() - t0) / band
+    rows = int(min(rows_total, max(1, seconds / max(per_row, 1e-9))))
+    blocks = 0
+    t0 = time.perf_counter()
+    while True:
+        r0 = 0
+        while r0 < rows_total and blocks < rows * bw:
+            r1 = min(rows_total, r0 + rows)
+            oracle.compress(fmt, img[4 * r0:4 * r1], w, min(h, 4 * r1) - 4 * r0, params, nthreads=nthreads)
+            blocks += (r1 - r0) * bw
+            r0 = r1
+        if time.perf_counter() - t0 >= seconds or blocks >= rows * bw:
+            break
+    dt = time.perf_counter() - t0
+    return blocks / dt / 1e6, blocks, dt
+
+
+# ---------------------------------------------------------------------------
+
+def headline_image(size, seed=0):
+    from texpresso_gb300 import workloads
+    return workloads.ramp_texture(size, size, seed=seed, alpha="ramp")
+
+
+def config_line(size):
+    nb = (size // 4) ** 2
+    return {"workload": "BC3 ClusterFit %dx%d RGBA8 (%d blocks), perceptual weights, weigh_colour_by_alpha=false"
+            % (size, size, nb),
+            "format": "BC3", "algorithm": "ClusterFit", "width": size, "height": size, "blocks": nb,
+            "input": "noisy per-block colour ramps (sigma 6, 10% flat), alpha ramps +-12 with 0/255 in 15%",
+            "l2": "inputs rotate over copies totalling > 3x L2 (129 MB); no flush needed"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from oracle import oracle
+    img = headline_image(args.size)
+    params = oracle.make_params(1, (0.2126, 0.7152, 0.0722), False)
+    cores = oracle.online_cores()
+    h, w = img.shape[:2]
+    bw = (w + 3) // 4
+    rows_total = (h + 3) // 4
+    # size each step so the whole run stays within ~2 minutes
+    budget = 120.0 / max(1, args.steps + args.warmup)
+    t0 = time.perf_counter()
+    oracle.compress(2, img[:16], w, 16, params)
+    per_row = (time.perf_counter() - t0) / 4
+    rows = int(max(1, min(rows_total, budget / max(per_row, 1e-9))))
+    for i in range(args.warmup):
+        oracle.compress(2, img[:4 * rows], w, 4 * rows, params)
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        r0 = (i * rows) % rows_total
+        r1 = min(rows_total, r0 + rows)
+        oracle.compress(2, img[4 * r0:4 * r1], w, 4 * (r1 - r0), params)
+    dt = time.perf_counter() - t0
+    blocks = 0
+    for i in range(args.steps):
+        r0 = (i * rows) % rows_total
+        blocks += (min(rows_total, r0 + rows) - r0) * bw
+    value = blocks / dt / 1e6
+    sample = "%d block rows (%d blocks) of the %dx%d texture per step, %d threads" % (rows, rows * bw, w, h, cores)
+    line = {"metric": METRIC, "value": round(value, 4), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt * 1e3 / args.steps, 4), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": config_line(args.size), "impl": "reference",
+            "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                             "sample": sample},
+            "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "note": "the reference is Rust and no cargo/rustc exists here or on the GPU box; its algorithm runs "
+                    "as the C oracle (oracle/texpresso_oracle.c) on all host cores"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args):
+    import torch
+    import texpresso_gb300 as tx
+    from texpresso_gb300 import replicas, workloads
+
+    rank, world_size, local_rank = replicas.world()
+    if world_size > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl", init_method="env://")
+    else:
+        torch.cuda.set_device(0)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    hbm_peak, sm_max_mhz, peak_kind = peaks()
+    fp32_peak_tops = 152 * 128 * sm_max_mhz * 1e6 / 1e12  # one FP32 op per lane per clock
+
+    size = args.size
+    img = headline_image(size, seed=rank)
+    params = tx.Params()  # ClusterFit, perceptual, no alpha weighting
+    run = DeviceRun(torch, tx, 2, [img], params)
+    nb = run.nblocks
+
+    clocks = Clocks(local_rank)
+    replicas.barrier(dev)
+    torch.cuda.synchronize()
+    clocks.start()
+    ms, launches = run.time(args.steps, args.warmup)
+    clk = clocks.stop()
+    torch.cuda.synchronize()
+    replicas.barrier(dev)
+    ms_max = replicas.max_over_ranks(ms, dev)
+    value = world_size * args.steps * nb / (ms_max * 1e-3) / 1e6
+    ms_step = ms_max / args.steps
+
+    # end to end through the drop-in host call
+    e2e_steps = max(3, min(args.steps, 50))
+    e2e_ms, h2d, d2h = e2e_time(torch, tx, 2, img, params, e2e_steps, max(3, args.warmup))
+    e2e_ms = replicas.max_over_ranks(e2e_ms, dev)
+    e2e_value = world_size * e2e_steps * nb / (e2e_ms * 1e-3) / 1e6
+
+    ops = cluster_ops(img, 2)
+    achieved_tops = ops / (ms_step * 1e-3) / 1e12
+    hbm_achieved = BYTES_PER_BLOCK[2] * nb / (ms_step * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded; the reference publishes no inputs)",
+        "config": config_line(size),
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "api": "tx_compress (C ABI, pinned host buffers)", "steps": e2e_steps},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp32", "achieved": round(achieved_tops, 3), "peak": round(fp32_peak_tops, 2),
+                     "unit": "TFLOP/s", "frac": round(achieved_tops / fp32_peak_tops, 4), "traffic": None,
+                     "work": "%d FP32 ops per launch = candidate evaluations x %d (compress4)" % (ops, OPS_CAND4),
+                     "peak_basis": "nominal: 152 SMs x 128 FP32 lanes x %.0f MHz (sm_max_mhz)" % sm_max_mhz},
+        "roofline_hbm": {"bound": "hbm", "achieved": round(hbm_achieved, 1), "peak": hbm_peak, "unit": "GB/s",
+                         "frac": round(hbm_achieved / hbm_peak, 4), "traffic": None,
+                         "basis": "80 B per block (64 B RGBA8 + 16 B BC3) x %d blocks; peak %s" % (nb, peak_kind)},
+        "clocks": clk,
+    }
+    traffic = os.path.join(ROOT, "profiles", "traffic.json")
+    if os.path.exists(traffic):
+        try:
+            with open(traffic) as f:
+                t = json.load(f)
+            key = "bc3_cluster_%d" % size
+            if key in t:
+                line["roofline"]["traffic"] = t[key]
+                line["roofline_hbm"]["traffic"] = t[key]
+        except (OSError, ValueError):
+            pass
+
+    if rank == 0 and world_size == 1:
+        from oracle import oracle
+        cores = oracle.online_cores()
+        cpu_v, cpu_blocks, cpu_dt = cpu_rate(oracle, 2, img, oracle.make_params(1), args.cpu_seconds)
+        line["cpu_baseline"] = {"value": round(cpu_v, 4), "unit": UNIT, "cores": cores, "kind": "port",
+                                "sample": "%d blocks of the same texture in %.1f s, %d threads, one block row per "
+                                          "task (C oracle, -O3 -ffp-contract=off)" % (cpu_blocks, cpu_dt, cores)}
+        line["speedup_vs_cpu"] = {"value": round(value / cpu_v, 1), "e2e": round(e2e_value / cpu_v, 1)}
+        if not args.no_extra:
+            line["extra"] = extras(torch, tx, oracle, args, hbm_peak, fp32_peak_tops)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world_size > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def extras(torch, tx, oracle, args, hbm_peak, fp32_peak):
+    """Other format/algorithm configurations, each beside the CPU oracle."""
+    from texpresso_gb300 import workloads
+    out = {}
+    steps = max(20, min(200, args.steps))
+    cpu_s = 2.5
+    c0 = workloads.ramp_texture(256, 256, seed=0)
+    c1 = headline_image(2048, seed=0)
+    cases = [
+        ("C0 BC1 ClusterFit 256x256", 0, c0, tx.Params(), 1, 4),
+        ("C1 BC3 RangeFit 2048x2048", 2, c1, tx.Params(algorithm=tx.Algorithm.RangeFit), 0, 4),
+        ("C1 BC3 ClusterFit alpha-weighted 2048x2048", 2, c1, tx.Params(weigh_colour_by_alpha=True), 1, 4),
+        ("C1 BC3 RangeFit alpha-weighted 2048x2048", 2, c1,
+         tx.Params(algorithm=tx.Algorithm.RangeFit, weigh_colour_by_alpha=True), 0, 4),
+        ("BC1 IterativeClusterFit 2048x2048", 0, workloads.ramp_texture(2048, 2048, seed=4),
+         tx.Params(algorithm=tx.Algorithm.IterativeClusterFit), 2, 4),
+    ]
+    noise = workloads.value_noise(4096, 4096, channels=2, seed=3)
+    rgba = workloads.expand_to_rgba(noise)
+    cases += [
+        ("C2 BC4 4096x4096 R8", 3, np.ascontiguousarray(noise[..., :1]), tx.Params(), 1, 1),
+        ("C2 BC5 4096x4096 RG8", 4, np.ascontiguousarray(noise), tx.Params(), 1, 2),
+        ("C2 BC4 4096x4096 RGBA8", 3, rgba, tx.Params(), 1, 4),
+        ("C2 BC5 4096x4096 RGBA8", 4, rgba, tx.Params(), 1, 4),
+    ]
+    for name, fmt, img, p, alg, ch in cases:
+        r = DeviceRun(torch, tx, fmt, [img], p, channels=ch)
+        ms, launches = r.time(steps, 3)
+        ms_step = ms / steps
+        v = r.nblocks / (ms_step * 1e-3) / 1e6
+        rec = {"mblocks_s": round(v, 2), "ms_per_step": round(ms_step, 5), "blocks": r.nblocks}
+        rgba_img = img if ch == 4 else workloads.expand_to_rgba(img)
+        op = oracle.make_params(alg, tuple(p.weights), p.weigh_colour_by_alpha)
+        cv, _, _ = cpu_rate(oracle, fmt, rgba_img, op, cpu_s)
+        rec["cpu_mblocks_s"] = round(cv, 4)
+        rec["speedup_vs_cpu"] = round(v / cv, 1)
+        bpb = BYTES_PER_BLOCK_NATIVE[fmt] if ch in (1, 2) else BYTES_PER_BLOCK[fmt]
+        gbs = bpb * r.nblocks / (ms_step * 1e-3) / 1e9
+        rec["hbm"] = {"achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 4), "bytes_per_block": bpb}
+        if alg == 1 and fmt < 3:
+            ops = cluster_ops(rgba_img, fmt)
+            tops = ops / (ms_step * 1e-3) / 1e12
+            rec["fp32"] = {"achieved_tops": round(tops, 3), "frac": round(tops / fp32_peak, 4)}
+        out[name] = rec
+        del r
+        torch.cuda.empty_cache()
+    return out
+
+
+def main():
+    args = parse()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,216 @@
+"""texpresso_gb300 -- GB300-native BCn block encoder behind texpresso's API.
+
+Python mirror of the reference crate's public interface (lib/src/lib.rs):
+``Format`` with ``compress``, ``compress_block_masked``, ``decompress``,
+``decompress_block``, ``block_size`` and ``compressed_size``; ``Params``;
+``Algorithm``; ``COLOUR_WEIGHTS_UNIFORM`` / ``COLOUR_WEIGHTS_PERCEPTUAL``;
+``num_blocks``.  Every call goes through the C ABI of
+``libtexpresso_gb300.so`` (include/texpresso_gb300.h) to sm_103a kernels.
+There is no CPU fallback: importing fails loudly if the library has not been
+built, and compute calls raise ``TexpressoError`` without a CUDA device.
+
+Where the reference panics (short output, zero width, partial trailing block)
+these functions raise ``TexpressoError`` carrying the C status code.
+
+Device-side entry points (``compress_device``, ``compress_blocks_device``,
+``decompress_device``) take raw device pointers and a CUDA stream handle so
+that callers holding GPU buffers (for example torch tensors) avoid host
+copies.
+"""
+import ctypes
+import enum
+import os
+from dataclasses import dataclass, field
+from typing import Sequence
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libtexpresso_gb300.so")
+
+if not os.path.exists(LIB_PATH):
+    raise ImportError(
+        "texpresso_gb300: %s is missing; build it first with "
+        "`python -c 'import __graft_entry__ as g; g.build()'` (needs nvcc)" % LIB_PATH)
+
+_lib = ctypes.CDLL(LIB_PATH)
+
+TX_OK = 0
+STATUS = {
+    -1: "TX_ERR_INVALID_FORMAT", -2: "TX_ERR_INVALID_ARGUMENT", -3: "TX_ERR_OUTPUT_TOO_SMALL",
+    -4: "TX_ERR_INPUT_TOO_SMALL", -5: "TX_ERR_CUDA", -6: "TX_ERR_NO_DEVICE", -7: "TX_ERR_TIMEOUT",
+    -8: "TX_ERR_OUT_OF_MEMORY", -9: "TX_ERR_MISALIGNED", -10: "TX_ERR_BUSY", -11: "TX_ERR_CANCELLED",
+}
+
+
+class TexpressoError(RuntimeError):
+    """Raised where the reference panics, or on a CUDA failure."""
+
+    def __init__(self, status, what=""):
+        self.status = status
+        msg = _lib.tx_status_string(status).decode()
+        if status == -5:
+            msg += " (cudaError %d)" % _lib.tx_last_cuda_error()
+        super().__init__("%s: %s [%s]" % (what or "texpresso", msg, STATUS.get(status, status)))
+
+
+class _CParams(ctypes.Structure):
+    _fields_ = [("algorithm", ctypes.c_int32), ("weights", ctypes.c_float * 3),
+                ("weigh_colour_by_alpha", ctypes.c_int32)]
+
+
+_u8p = ctypes.POINTER(ctypes.c_uint8)
+_sz = ctypes.c_size_t
+_vp = ctypes.c_void_p
+_lib.tx_status_string.restype = ctypes.c_char_p
+_lib.tx_status_string.argtypes = [ctypes.c_int]
+_lib.tx_params_default.argtypes = [ctypes.POINTER(_CParams)]
+_lib.tx_num_blocks.restype = _sz
+_lib.tx_num_blocks.argtypes = [_sz]
+_lib.tx_block_size.restype = _sz
+_lib.tx_block_size.argtypes = [ctypes.c_int]
+_lib.tx_compressed_size.restype = _sz
+_lib.tx_compressed_size.argtypes = [ctypes.c_int, _sz, _sz]
+_lib.tx_compress.argtypes = [ctypes.c_int, _vp, _sz, _sz, _sz, ctypes.POINTER(_CParams), _vp, _sz]
+_lib.tx_compress_block_masked.argtypes = [ctypes.c_int, _vp, ctypes.c_uint32, ctypes.POINTER(_CParams), _vp, _sz]
+_lib.tx_compress_device.argtypes = [ctypes.c_int, _vp, _sz, ctypes.c_int, _sz, _sz, ctypes.POINTER(_CParams),
+                                    _vp, _sz, _vp]
+_lib.tx_compress_blocks_device.argtypes = [ctypes.c_int, _vp, _vp, _sz, ctypes.POINTER(_CParams), _vp, _vp]
+_lib.tx_decompress.argtypes = [ctypes.c_int, _vp, _sz, _sz, _sz, _vp, _sz]
+_lib.tx_decompress_block.argtypes = [ctypes.c_int, _vp, _sz, _vp]
+_lib.tx_decompress_device.argtypes = [ctypes.c_int, _vp, _sz, _sz, _sz, _vp, _sz, _vp]
+_lib.tx_last_cuda_error.restype = ctypes.c_int
+_lib.tx_kernel_launch_count.restype = ctypes.c_uint64
+
+
+def _check(rc, what):
+    if rc != TX_OK:
+        raise TexpressoError(rc, what)
+
+
+class Algorithm(enum.IntEnum):
+    """lib/src/lib.rs:49-59"""
+    RangeFit = 0
+    ClusterFit = 1
+    IterativeClusterFit = 2
+
+
+COLOUR_WEIGHTS_UNIFORM = (1.0, 1.0, 1.0)               # lib/src/lib.rs:71
+COLOUR_WEIGHTS_PERCEPTUAL = (0.2126, 0.7152, 0.0722)   # lib/src/lib.rs:74
+
+
+@dataclass
+class Params:
+    """lib/src/lib.rs:76-100 (defaults: ClusterFit, perceptual weights, no alpha weighting)."""
+    algorithm: Algorithm = Algorithm.ClusterFit
+    weights: Sequence[float] = field(default_factory=lambda: COLOUR_WEIGHTS_PERCEPTUAL)
+    weigh_colour_by_alpha: bool = False
+
+    def _c(self):
+        p = _CParams()
+        p.algorithm = int(self.algorithm)
+        for i in range(3):
+            p.weights[i] = float(self.weights[i])
+        p.weigh_colour_by_alpha = 1 if self.weigh_colour_by_alpha else 0
+        return p
+
+
+def num_blocks(size):
+    """lib/src/lib.rs:103-105"""
+    return int(_lib.tx_num_blocks(size))
+
+
+def _buffer(obj, writable):
+    """(address, length) of a C-contiguous bytes-like or numpy buffer, without copying."""
+    if isinstance(obj, np.ndarray):
+        if not obj.flags.c_contiguous:
+            raise ValueError("buffer must be C-contiguous")
+        if writable and not obj.flags.writeable:
+            raise TypeError("output buffer is read-only")
+        return (obj.ctypes.data if obj.nbytes else None), obj.nbytes
+    mv = memoryview(obj)
+    if not mv.contiguous:
+        raise ValueError("buffer must be contiguous")
+    if writable and mv.readonly:
+        raise TypeError("output buffer is read-only")
+    a = np.frombuffer(mv, dtype=np.uint8)
+    return (a.ctypes.data if a.size else None), a.size
+
+
+class Format(enum.IntEnum):
+    """lib/src/lib.rs:39-46 and the methods of impl Format (:117-336)."""
+    Bc1 = 0
+    Bc2 = 1
+    Bc3 = 2
+    Bc4 = 3
+    Bc5 = 4
+
+    def block_size(self):
+        """lib/src/lib.rs:159-168"""
+        return int(_lib.tx_block_size(int(self)))
+
+    def compressed_size(self, width, height):
+        """lib/src/lib.rs:175-179"""
+        return int(_lib.tx_compressed_size(int(self), width, height))
+
+    def compress(self, rgba, width, height, params, output):
+        """Format::compress (lib/src/lib.rs:287-335): RGBA8 in, blocks written into output."""
+        src, slen = _buffer(rgba, False)
+        dst, dlen = _buffer(output, True)
+        rc = _lib.tx_compress(int(self), src, slen, width, height, ctypes.byref(params._c()), dst, dlen)
+        _check(rc, "Format.compress")
+
+    def compress_block_masked(self, rgba, mask, params, output):
+        """Format::compress_block_masked (lib/src/lib.rs:188-234)."""
+        src, slen = _buffer(rgba, False)
+        if slen < 64:
+            raise TexpressoError(-4, "Format.compress_block_masked")
+        dst, dlen = _buffer(output, True)
+        rc = _lib.tx_compress_block_masked(int(self), src, mask & 0xFFFFFFFF, ctypes.byref(params._c()), dst, dlen)
+        _check(rc, "Format.compress_block_masked")
+
+    def decompress(self, data, width, height, output):
+        """Format::decompress (lib/src/lib.rs:124-156)."""
+        src, slen = _buffer(data, False)
+        dst, dlen = _buffer(output, True)
+        rc = _lib.tx_decompress(int(self), src, slen, width, height, dst, dlen)
+        _check(rc, "Format.decompress")
+
+    def decompress_block(self, block):
+        """Format::decompress_block (lib/src/lib.rs:240-277): returns 64 RGBA8 bytes."""
+        out = bytearray(64)
+        src, slen = _buffer(block, False)
+        dst, _ = _buffer(out, True)
+        rc = _lib.tx_decompress_block(int(self), src, slen, dst)
+        _check(rc, "Format.decompress_block")
+        return bytes(out)
+
+
+def compress_device(fmt, src_ptr, src_pitch, channels, width, height, params, out_ptr, out_len, stream=0):
+    """Stream-ordered compress of a device image (tx_compress_device)."""
+    _check(_lib.tx_compress_device(int(fmt), src_ptr, src_pitch, channels, width, height,
+                                   ctypes.byref(params._c()), out_ptr, out_len, stream or None),
+           "compress_device")
+
+
+def compress_blocks_device(fmt, blocks_ptr, masks_ptr, nblocks, params, out_ptr, stream=0):
+    """Stream-ordered compress of nblocks x 64-byte RGBA8 blocks (tx_compress_blocks_device)."""
+    _check(_lib.tx_compress_blocks_device(int(fmt), blocks_ptr, masks_ptr or None, nblocks,
+                                          ctypes.byref(params._c()), out_ptr, stream or None),
+           "compress_blocks_device")
+
+
+def decompress_device(fmt, data_ptr, data_len, width, height, out_ptr, out_pitch, stream=0):
+    """Stream-ordered decode into a device RGBA8 image (tx_decompress_device)."""
+    _check(_lib.tx_decompress_device(int(fmt), data_ptr, data_len, width, height, out_ptr, out_pitch,
+                                     stream or None), "decompress_device")
+
+
+def kernel_launch_count():
+    """Kernels this library has launched in this process."""
+    return int(_lib.tx_kernel_launch_count())
+
+
+def library():
+    """The loaded ctypes library (for tests of the raw C ABI)."""
+    return _lib

@@ -1,0 +1,293 @@
+// tx_device.cuh -- device-side building blocks shared by the BCn kernels.
+//
+// Every translation unit that includes this file is compiled with
+// -fmad=false -prec-div=true -prec-sqrt=true -ftz=false: a*b+c is never fused,
+// division and square root are IEEE round-to-nearest, subnormals are kept.
+// That reproduces the reference's scalar f32 arithmetic (Rust never contracts;
+// lib/src/math/vec3.rs, lib/src/math/vec4.rs) bit for bit.
+#pragma once
+
+#include <cstdint>
+#include <cfloat>
+#include <cuda_runtime.h>
+
+namespace tx {
+
+enum Format : int { BC1 = 0, BC2 = 1, BC3 = 2, BC4 = 3, BC5 = 4 };
+enum Algorithm : int { RANGE_FIT = 0, CLUSTER_FIT = 1, ITERATIVE_CLUSTER_FIT = 2 };
+
+// Kernel-side copy of the caller's Params (lib/src/lib.rs:76-90).
+struct DevParams {
+    float w[3];
+    int alpha_weighted;
+};
+
+// Where a kernel reads its pixels from.
+struct SrcDesc {
+    const uint8_t *base;   // image (mode 0) or packed 64-byte blocks (mode 1)
+    const uint32_t *masks; // mode 1: per-block valid masks (nullptr = all valid)
+    size_t pitch;          // mode 0: bytes between rows
+    uint32_t width, height;
+    uint32_t blocks_wide;  // num_blocks(width)
+    int channels;          // 4 = RGBA8, 1 = R8, 2 = RG8
+    int vec16;             // mode 0, RGBA8: rows 16-byte aligned -> 128-bit loads
+    int mode;              // 0 image, 1 block list
+};
+
+__host__ __device__ constexpr int block_bytes(int fmt) { return (fmt == BC1 || fmt == BC4) ? 8 : 16; }
+
+// ---------------------------------------------------------------------------
+// exact scalar helpers (lib/src/math.rs:100-102, lib/src/math/vec4.rs:94-110)
+
+__device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }   // == 1.0f / x
+__device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
+__device__ __forceinline__ float sqrt_rn(float x) { return __fsqrt_rn(x); }
+
+// f32_to_i32_clamped: roundf(a).max(0).min(limit) as i32 (max/min drop NaN).
+__device__ __forceinline__ int f32_to_i32_clamped(float a, int limit) {
+    return (int)fminf(fmaxf(roundf(a), 0.0f), (float)limit);
+}
+
+// u8 -> [0,1] exactly as colourset.rs:65-67 (f32::from(v) / 255f32).
+__device__ __forceinline__ float unorm8(uint32_t v) { return div_rn((float)v, 255.0f); }
+
+// ---------------------------------------------------------------------------
+// packing (lib/src/colourblock.rs:28-94)
+
+__device__ __forceinline__ uint32_t pack_565(float x, float y, float z) {
+    uint32_t r = (uint32_t)f32_to_i32_clamped(31.0f * x, 31);
+    uint32_t g = (uint32_t)f32_to_i32_clamped(63.0f * y, 63);
+    uint32_t b = (uint32_t)f32_to_i32_clamped(31.0f * z, 31);
+    return (r << 11) | (g << 5) | b;
+}
+
+// Swap 2-bit indices 0 <-> 1 (write3's remap), 16 packed indices at once.
+__device__ __forceinline__ uint32_t swap01_2bit(uint32_t w) {
+    // an index is 0 or 1 when its high bit is clear; flipping its low bit swaps it
+    uint32_t hi = (w >> 1) & 0x55555555u;
+    return w ^ (~hi & 0x55555555u);
+}
+
+// write3: endpoints a,b (565) and 16 2-bit indices (pixel i at bits 2i).
+__device__ __forceinline__ uint2 write3(uint32_t a, uint32_t b, uint32_t idx) {
+    if (a > b) { uint32_t t = a; a = b; b = t; idx = swap01_2bit(idx); }
+    return make_uint2(a | (b << 16), idx);
+}
+
+// write4: a<b swaps and flips bit 0 of every index; a==b zeroes the indices.
+__device__ __forceinline__ uint2 write4(uint32_t a, uint32_t b, uint32_t idx) {
+    if (a < b) { uint32_t t = a; a = b; b = t; idx ^= 0x55555555u; }
+    else if (a == b) { idx = 0; }
+    return make_uint2(a | (b << 16), idx);
+}
+
+// ---------------------------------------------------------------------------
+// block gather (lib/src/lib.rs:305-333): 16 RGBA8 pixels + valid mask.
+
+__device__ __forceinline__ uint32_t ld_u32_any(const uint8_t *p) {
+    // p is 4-byte aligned when the image base is; fall back to bytes otherwise
+    if ((reinterpret_cast<uintptr_t>(p) & 3u) == 0) return __ldg(reinterpret_cast<const uint32_t *>(p));
+    return (uint32_t)p[0] | ((uint32_t)p[1] << 8) | ((uint32_t)p[2] << 16) | ((uint32_t)p[3] << 24);
+}
+
+// Load the 16 pixels of block `b` into px[] (pixel 4*y+x), return the mask.
+// Masked pixels read as 0; the reference never looks at them.
+__device__ __forceinline__ uint32_t load_block_rgba(const SrcDesc &s, size_t b, uint32_t (&px)[16]) {
+    if (s.mode == 1) {
+        const uint4 *q = reinterpret_cast<const uint4 *>(s.base + 64 * b);
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            uint4 v = __ldg(q + r);
+            px[4 * r + 0] = v.x; px[4 * r + 1] = v.y; px[4 * r + 2] = v.z; px[4 * r + 3] = v.w;
+        }
+        return s.masks ? (__ldg(s.masks + b) & 0xFFFFu) : 0xFFFFu;
+    }
+    const uint32_t bx = (uint32_t)(b % s.blocks_wide), by = (uint32_t)(b / s.blocks_wide);
+    const uint32_t x0 = 4 * bx;
+    uint32_t mask = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const uint32_t y = 4 * by + r;
+        if (y < s.height) {
+            const uint8_t *row = s.base + (size_t)y * s.pitch + 4 * (size_t)x0;
+            if (s.vec16 && x0 + 4 <= s.width) {
+                uint4 v = __ldcs(reinterpret_cast<const uint4 *>(row));
+                px[4 * r + 0] = v.x; px[4 * r + 1] = v.y; px[4 * r + 2] = v.z; px[4 * r + 3] = v.w;
+                mask |= 0xFu << (4 * r);
+            } else {
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    if (x0 + c < s.width) { px[4 * r + c] = ld_u32_any(row + 4 * c); mask |= 1u << (4 * r + c); }
+                    else px[4 * r + c] = 0;
+                }
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 4; ++c) px[4 * r + c] = 0;
+        }
+    }
+    return mask;
+}
+
+// Expand a 4-bit pixel mask into byte lanes (0xFF per valid pixel).
+__device__ __forceinline__ uint32_t nibble_to_bytemask(uint32_t nib) {
+    return ((nib * 0x00204081u) & 0x01010101u) * 0xFFu;
+}
+
+// ---------------------------------------------------------------------------
+// BC2 alpha (lib/src/alpha.rs:27-51)
+
+__device__ __forceinline__ uint32_t bc2_quant(uint32_t a) {
+    return (uint32_t)f32_to_i32_clamped((float)a * (15.0f / 255.0f), 15);
+}
+
+__device__ __forceinline__ uint2 encode_bc2_alpha(const uint32_t (&px)[16], uint32_t mask) {
+    uint32_t lo = 0, hi = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        uint32_t q = ((mask >> i) & 1u) ? bc2_quant(px[i] >> 24) : 0u;
+        if (i < 8) lo |= q << (4 * i); else hi |= q << (4 * (i - 8));
+    }
+    return make_uint2(lo, hi);
+}
+
+// ---------------------------------------------------------------------------
+// BC3/BC4/BC5 alpha block (lib/src/alpha.rs:70-256) with SIMD-in-word search.
+//
+// v[r] holds the channel values of pixels 4r..4r+3 (byte c = pixel 4r+c).
+// For every pixel the reference picks the first code with the least squared
+// distance; |v-c| orders codes the same way (and keeps ties), so each 32-bit
+// word tracks four pixels with per-byte min/compare/select.  Errors are sums
+// of squared byte distances (dp4a), which is exact integer arithmetic.
+
+struct AlphaFit {
+    uint32_t err;
+    uint32_t idx[4];  // per-byte code index
+};
+
+__device__ __forceinline__ AlphaFit fit_codes8(const uint32_t (&v)[4], const uint32_t (&vm)[4],
+                                               const uint32_t (&codes)[8]) {
+    AlphaFit f;
+    uint32_t best[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) { best[r] = __vabsdiffu4(v[r], codes[0] * 0x01010101u); f.idx[r] = 0; }
+#pragma unroll
+    for (int j = 1; j < 8; ++j) {
+        const uint32_t c4 = codes[j] * 0x01010101u, j4 = (uint32_t)j * 0x01010101u;
+#pragma unroll
+        for (int r = 0; r < 4; ++r) {
+            uint32_t d = __vabsdiffu4(v[r], c4);
+            uint32_t lt = __vcmpltu4(d, best[r]);
+            best[r] = __vminu4(best[r], d);
+            f.idx[r] = (f.idx[r] & ~lt) | (j4 & lt);
+        }
+    }
+    uint32_t e = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        f.idx[r] &= vm[r];              // masked pixels take code 0 (alpha.rs:92-95)
+        const uint32_t d = best[r] & vm[r];
+        e = __dp4a(d, d, e);
+    }
+    f.err = e;
+    return f;
+}
+
+__device__ __forceinline__ uint32_t bytes_min(uint32_t w) {
+    w = __vminu4(w, w >> 16);
+    w = __vminu4(w, w >> 8);
+    return w & 0xFFu;
+}
+__device__ __forceinline__ uint32_t bytes_max(uint32_t w) {
+    w = __vmaxu4(w, w >> 16);
+    w = __vmaxu4(w, w >> 8);
+    return w & 0xFFu;
+}
+
+// fix_range (alpha.rs:70-77); min <= max on entry.
+__device__ __forceinline__ void fix_range(int &mn, int &mx, int steps) {
+    if (mx - mn < steps) mx = min(mn + steps, 255);
+    if (mx - mn < steps) mn = max(mx - steps, 0);
+}
+
+// 3-bit indices of four pixels (one per byte) -> 12 bits.
+__device__ __forceinline__ uint32_t pack3x4(uint32_t w) {
+    return (w & 0x7u) | ((w >> 5) & 0x38u) | ((w >> 10) & 0x1C0u) | ((w >> 15) & 0xE00u);
+}
+
+__device__ __forceinline__ uint2 write_alpha_block(uint32_t a0, uint32_t a1, const uint32_t (&idx)[4]) {
+    const uint32_t lo = pack3x4(idx[0]) | (pack3x4(idx[1]) << 12);  // pixels 0..7
+    const uint32_t hi = pack3x4(idx[2]) | (pack3x4(idx[3]) << 12);  // pixels 8..15
+    return make_uint2(a0 | (a1 << 8) | ((lo & 0xFFFFu) << 16), (lo >> 16) | (hi << 8));
+}
+
+// compress_bc3 for one channel: v = 16 packed values, mask = valid pixels.
+__device__ __forceinline__ uint2 encode_bc3_alpha(const uint32_t (&v)[4], uint32_t mask) {
+    uint32_t vm[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) vm[r] = nibble_to_bytemask((mask >> (4 * r)) & 0xFu);
+    uint32_t mn7 = 0xFFFFFFFFu, mx7 = 0, mn5 = 0xFFFFFFFFu, mx5 = 0;
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const uint32_t is0 = __vcmpeq4(v[r], 0u), is255 = __vcmpeq4(v[r], 0xFFFFFFFFu);
+        mn7 = __vminu4(mn7, v[r] | ~vm[r]);
+        mx7 = __vmaxu4(mx7, v[r] & vm[r]);
+        mn5 = __vminu4(mn5, v[r] | ~vm[r] | is0);
+        mx5 = __vmaxu4(mx5, v[r] & vm[r] & ~is255);
+    }
+    int min7 = (int)bytes_min(mn7), max7 = (int)bytes_max(mx7);
+    int min5 = (int)bytes_min(mn5), max5 = (int)bytes_max(mx5);
+    if (min5 > max5) min5 = max5;
+    if (min7 > max7) min7 = max7;
+    fix_range(min5, max5, 5);
+    fix_range(min7, max7, 7);
+    uint32_t c5[8], c7[8];
+    c5[0] = (uint32_t)min5; c5[1] = (uint32_t)max5;
+#pragma unroll
+    for (int i = 1; i < 5; ++i) c5[1 + i] = (uint32_t)(((5 - i) * min5 + i * max5) / 5);
+    c5[6] = 0; c5[7] = 255;
+    // codes7[0..2] are min5/max5 (alpha.rs:237-239), the rest span min7..max7
+    c7[0] = (uint32_t)min5; c7[1] = (uint32_t)max5;
+#pragma unroll
+    for (int i = 1; i < 7; ++i) c7[1 + i] = (uint32_t)(((7 - i) * min7 + i * max7) / 7);
+    const AlphaFit f5 = fit_codes8(v, vm, c5);
+    const AlphaFit f7 = fit_codes8(v, vm, c7);
+    uint32_t out[4];
+    if (f5.err <= f7.err) {
+        // write_alpha_block5: a0 > a1 cannot occur after fix_range; kept for fidelity
+        if (min5 > max5) {
+#pragma unroll
+            for (int r = 0; r < 4; ++r) {
+                uint32_t w = f5.idx[r], o = 0;
+#pragma unroll
+                for (int c = 0; c < 4; ++c) {
+                    uint32_t x = (w >> (8 * c)) & 0xFFu;
+                    x = x == 0 ? 1u : x == 1 ? 0u : (x <= 5 ? 7u - x : x);
+                    o |= x << (8 * c);
+                }
+                out[r] = o;
+            }
+            return write_alpha_block((uint32_t)max5, (uint32_t)min5, out);
+        }
+        return write_alpha_block((uint32_t)min5, (uint32_t)max5, f5.idx);
+    }
+    // write_alpha_block7: min7 < max7 always holds here; 0<->1, x -> 9-x is (9-x)&7
+    if (min7 < max7) {
+#pragma unroll
+        for (int r = 0; r < 4; ++r) out[r] = (0x09090909u - f7.idx[r]) & 0x07070707u;
+        return write_alpha_block((uint32_t)max7, (uint32_t)min7, out);
+    }
+    return write_alpha_block((uint32_t)min7, (uint32_t)max7, f7.idx);
+}
+
+// Gather one byte channel of 16 RGBA8 pixels into 4 packed words.
+__device__ __forceinline__ void channel_words(const uint32_t (&px)[16], int ch, uint32_t (&v)[4]) {
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        const int s = 8 * ch;
+        v[r] = ((px[4 * r] >> s) & 0xFFu) | (((px[4 * r + 1] >> s) & 0xFFu) << 8) |
+               (((px[4 * r + 2] >> s) & 0xFFu) << 16) | (((px[4 * r + 3] >> s) & 0xFFu) << 24);
+    }
+}
+
+}  // namespace tx
