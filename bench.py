@@ -65,6 +65,9 @@ def parse():
     ap.add_argument("--no-extra", action="store_true", help="skip the per-format extra lines")
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
+    ap.add_argument("--case", default=None,
+                    help="time one extra workload only (device timing, no CPU leg); for profiling: " +
+                         ", ".join(CASES))
     return ap.parse_args()
 
 
@@ -157,6 +160,20 @@ class Clocks:
         return {"sm_mhz": statistics.median(r[0] for r in load), "sm_max_mhz": max(r[1] for r in rows),
                 "power_w_max": max(r[2] for r in rows), "samples": len(rows), "samples_under_load": len(load),
                 "reasons": sorted(reasons)}
+
+
+def dram_traffic():
+    """Per-launch DRAM bytes from the committed ncu summaries (profiles/dram_traffic.txt)."""
+    out = {}
+    try:
+        with open(os.path.join(ROOT, "profiles", "dram_traffic.txt")) as f:
+            for line in f:
+                line = line.split("#")[0].split()
+                if len(line) >= 2:
+                    out[line[0]] = int(line[1])
+    except (OSError, ValueError):
+        pass
+    return out
 
 
 def peaks():
@@ -384,17 +401,10 @@ def run_ours(args):
                          "basis": "80 B per block (64 B RGBA8 + 16 B BC3) x %d blocks; peak %s" % (nb, peak_kind)},
         "clocks": clk,
     }
-    traffic = os.path.join(ROOT, "profiles", "traffic.json")
-    if os.path.exists(traffic):
-        try:
-            with open(traffic) as f:
-                t = json.load(f)
-            key = "bc3_cluster_%d" % size
-            if key in t:
-                line["roofline"]["traffic"] = t[key]
-                line["roofline_hbm"]["traffic"] = t[key]
-        except (OSError, ValueError):
-            pass
+    traffic = dram_traffic().get("bc3_cluster_%d" % size)
+    if traffic is not None:
+        line["roofline"]["traffic"] = traffic
+        line["roofline_hbm"]["traffic"] = traffic
 
     if rank == 0 and world_size == 1:
         from oracle import oracle
@@ -414,53 +424,101 @@ def run_ours(args):
     return 0
 
 
+CASES = ["c0_bc1_cluster", "c1_bc3_range", "c1_bc3_cluster_aw", "c1_bc3_range_aw", "bc1_iter_cluster",
+         "c2_bc4_r8", "c2_bc5_rg8", "c2_bc4_rgba", "c2_bc5_rgba", "c1_bc3_cluster"]
+
+
+def extra_cases(tx, names=None):
+    """(key, label, format, image, Params, oracle algorithm, channels) of the other configurations."""
+    from texpresso_gb300 import workloads
+    names = names or CASES[:-1]
+    out = []
+    cache = {}
+
+    def img(kind):
+        if kind not in cache:
+            if kind == "c0":
+                cache[kind] = workloads.ramp_texture(256, 256, seed=0)
+            elif kind == "c1":
+                cache[kind] = headline_image(2048, seed=0)
+            elif kind == "iter":
+                cache[kind] = workloads.ramp_texture(2048, 2048, seed=4)
+            elif kind == "noise":
+                cache[kind] = workloads.value_noise(4096, 4096, channels=2, seed=3)
+        return cache[kind]
+
+    P = tx.Params
+    R, C, I = tx.Algorithm.RangeFit, tx.Algorithm.ClusterFit, tx.Algorithm.IterativeClusterFit
+    table = {
+        "c0_bc1_cluster": ("C0 BC1 ClusterFit 256x256", 0, lambda: img("c0"), P(), 1, 4),
+        "c1_bc3_range": ("C1 BC3 RangeFit 2048x2048", 2, lambda: img("c1"), P(algorithm=R), 0, 4),
+        "c1_bc3_cluster_aw": ("C1 BC3 ClusterFit alpha-weighted 2048x2048", 2, lambda: img("c1"),
+                              P(weigh_colour_by_alpha=True), 1, 4),
+        "c1_bc3_range_aw": ("C1 BC3 RangeFit alpha-weighted 2048x2048", 2, lambda: img("c1"),
+                            P(algorithm=R, weigh_colour_by_alpha=True), 0, 4),
+        "bc1_iter_cluster": ("BC1 IterativeClusterFit 2048x2048", 0, lambda: img("iter"), P(algorithm=I), 2, 4),
+        "c2_bc4_r8": ("C2 BC4 4096x4096 R8", 3, lambda: np.ascontiguousarray(img("noise")[..., :1]), P(), 1, 1),
+        "c2_bc5_rg8": ("C2 BC5 4096x4096 RG8", 4, lambda: np.ascontiguousarray(img("noise")), P(), 1, 2),
+        "c2_bc4_rgba": ("C2 BC4 4096x4096 RGBA8", 3, lambda: workloads.expand_to_rgba(img("noise")), P(), 1, 4),
+        "c2_bc5_rgba": ("C2 BC5 4096x4096 RGBA8", 4, lambda: workloads.expand_to_rgba(img("noise")), P(), 1, 4),
+        "c1_bc3_cluster": ("C1 BC3 ClusterFit 2048x2048", 2, lambda: img("c1"), P(), 1, 4),
+    }
+    for k in names:
+        label, fmt, mk, p, alg, ch = table[k]
+        out.append((k, label, fmt, mk(), p, alg, ch))
+    return out
+
+
+def time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak):
+    from texpresso_gb300 import workloads
+    r = DeviceRun(torch, tx, fmt, [img], p, channels=ch)
+    ms, launches = r.time(steps, 3)
+    ms_step = ms / steps
+    v = r.nblocks / (ms_step * 1e-3) / 1e6
+    rec = {"mblocks_s": round(v, 2), "ms_per_step": round(ms_step, 5), "blocks": r.nblocks,
+           "gpu_launches": launches}
+    bpb = BYTES_PER_BLOCK_NATIVE[fmt] if ch in (1, 2) else BYTES_PER_BLOCK[fmt]
+    gbs = bpb * r.nblocks / (ms_step * 1e-3) / 1e9
+    rec["hbm"] = {"achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 4), "bytes_per_block": bpb}
+    if alg == 1 and fmt < 3:
+        rgba_img = img if ch == 4 else workloads.expand_to_rgba(img)
+        ops = cluster_ops(rgba_img, fmt)
+        tops = ops / (ms_step * 1e-3) / 1e12
+        rec["fp32"] = {"achieved_tops": round(tops, 3), "frac": round(tops / fp32_peak, 4)}
+    del r
+    torch.cuda.empty_cache()
+    return rec
+
+
 def extras(torch, tx, oracle, args, hbm_peak, fp32_peak):
     """Other format/algorithm configurations, each beside the CPU oracle."""
     from texpresso_gb300 import workloads
     out = {}
     steps = max(20, min(200, args.steps))
-    cpu_s = 2.5
-    c0 = workloads.ramp_texture(256, 256, seed=0)
-    c1 = headline_image(2048, seed=0)
-    cases = [
-        ("C0 BC1 ClusterFit 256x256", 0, c0, tx.Params(), 1, 4),
-        ("C1 BC3 RangeFit 2048x2048", 2, c1, tx.Params(algorithm=tx.Algorithm.RangeFit), 0, 4),
-        ("C1 BC3 ClusterFit alpha-weighted 2048x2048", 2, c1, tx.Params(weigh_colour_by_alpha=True), 1, 4),
-        ("C1 BC3 RangeFit alpha-weighted 2048x2048", 2, c1,
-         tx.Params(algorithm=tx.Algorithm.RangeFit, weigh_colour_by_alpha=True), 0, 4),
-        ("BC1 IterativeClusterFit 2048x2048", 0, workloads.ramp_texture(2048, 2048, seed=4),
-         tx.Params(algorithm=tx.Algorithm.IterativeClusterFit), 2, 4),
-    ]
-    noise = workloads.value_noise(4096, 4096, channels=2, seed=3)
-    rgba = workloads.expand_to_rgba(noise)
-    cases += [
-        ("C2 BC4 4096x4096 R8", 3, np.ascontiguousarray(noise[..., :1]), tx.Params(), 1, 1),
-        ("C2 BC5 4096x4096 RG8", 4, np.ascontiguousarray(noise), tx.Params(), 1, 2),
-        ("C2 BC4 4096x4096 RGBA8", 3, rgba, tx.Params(), 1, 4),
-        ("C2 BC5 4096x4096 RGBA8", 4, rgba, tx.Params(), 1, 4),
-    ]
-    for name, fmt, img, p, alg, ch in cases:
-        r = DeviceRun(torch, tx, fmt, [img], p, channels=ch)
-        ms, launches = r.time(steps, 3)
-        ms_step = ms / steps
-        v = r.nblocks / (ms_step * 1e-3) / 1e6
-        rec = {"mblocks_s": round(v, 2), "ms_per_step": round(ms_step, 5), "blocks": r.nblocks}
+    for key, label, fmt, img, p, alg, ch in extra_cases(tx):
+        rec = time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak)
         rgba_img = img if ch == 4 else workloads.expand_to_rgba(img)
         op = oracle.make_params(alg, tuple(p.weights), p.weigh_colour_by_alpha)
-        cv, _, _ = cpu_rate(oracle, fmt, rgba_img, op, cpu_s)
+        cv, _, _ = cpu_rate(oracle, fmt, rgba_img, op, 2.5)
         rec["cpu_mblocks_s"] = round(cv, 4)
-        rec["speedup_vs_cpu"] = round(v / cv, 1)
-        bpb = BYTES_PER_BLOCK_NATIVE[fmt] if ch in (1, 2) else BYTES_PER_BLOCK[fmt]
-        gbs = bpb * r.nblocks / (ms_step * 1e-3) / 1e9
-        rec["hbm"] = {"achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 4), "bytes_per_block": bpb}
-        if alg == 1 and fmt < 3:
-            ops = cluster_ops(rgba_img, fmt)
-            tops = ops / (ms_step * 1e-3) / 1e12
-            rec["fp32"] = {"achieved_tops": round(tops, 3), "frac": round(tops / fp32_peak, 4)}
-        out[name] = rec
-        del r
-        torch.cuda.empty_cache()
+        rec["speedup_vs_cpu"] = round(rec["mblocks_s"] / cv, 1)
+        out[label] = rec
     return out
+
+
+def run_case(args):
+    """One workload, device timing only (used for ncu captures)."""
+    import torch
+    import texpresso_gb300 as tx
+    torch.cuda.set_device(0)
+    hbm_peak, sm_max_mhz, _ = peaks()
+    fp32_peak = 152 * 128 * sm_max_mhz * 1e6 / 1e12
+    (key, label, fmt, img, p, alg, ch), = extra_cases(tx, [args.case])
+    rec = time_case(torch, tx, fmt, img, p, alg, ch, args.steps, hbm_peak, fp32_peak)
+    rec["case"] = key
+    rec["label"] = label
+    print(json.dumps(rec), flush=True)
+    return 0
 
 
 def main():
@@ -469,6 +527,8 @@ def main():
         args.warmup = 3
     if args.impl == "reference":
         return run_reference(args)
+    if args.case:
+        return run_case(args)
     return run_ours(args)
 
 
