@@ -65,6 +65,7 @@ def parse():
     ap.add_argument("--no-extra", action="store_true", help="skip the per-format extra lines")
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
+    ap.add_argument("--batched-only", action="store_true", help="run only the config-3 batched comparison")
     ap.add_argument("--case", default=None,
                     help="time one extra workload only (device timing, no CPU leg); for profiling: " +
                          ", ".join(CASES))
@@ -416,6 +417,7 @@ def run_ours(args):
         line["speedup_vs_cpu"] = {"value": round(value / cpu_v, 1), "e2e": round(e2e_value / cpu_v, 1)}
         if not args.no_extra:
             line["extra"] = extras(torch, tx, oracle, args, hbm_peak, fp32_peak_tops)
+            line["batched"] = batched(torch, tx, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world_size > 1:
@@ -506,6 +508,76 @@ def extras(torch, tx, oracle, args, hbm_peak, fp32_peak):
     return out
 
 
+def batched(torch, tx, args, n_textures=1000):
+    """Config 3: n textures (sides log-uniform 4..4096, mip chains, BC1/BC3/BC5 x
+    RangeFit/ClusterFit/IterativeClusterFit) as one autotuned batch launch
+    (CUDA graph) against one tx_compress_device call per texture level."""
+    from texpresso_gb300 import workloads
+    from texpresso_gb300.texture_set import TextureSet, same
+    t0 = time.perf_counter()
+    specs = workloads.batch_specs(n_textures, seed=0)
+    ts = TextureSet(specs, device="cuda")
+    torch.cuda.synchronize()
+    gen_s = time.perf_counter() - t0
+    s = torch.cuda.Stream()
+    b = tx.Batch(ts.items())
+    info = b.info()
+    t0 = time.perf_counter()
+    chosen = b.autotune(s.cuda_stream, repeats=1)
+    tune_s = time.perf_counter() - t0
+
+    def graph_of(fn):
+        fn()
+        torch.cuda.synchronize()
+        g = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(g, stream=s):
+            fn()
+        torch.cuda.synchronize()
+        return g
+
+    def time_graph(g, reps):
+        g.replay()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with torch.cuda.stream(s):
+            e0.record(s)
+            for _ in range(reps):
+                g.replay()
+            e1.record(s)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    reps = 3
+    gb = graph_of(lambda: b.launch(s.cuda_stream))
+    batch_ms = time_graph(gb, reps)
+    ref = ts.snapshot()
+    ts.clear_outputs()
+    # plain form, eager: the host loop of per-level calls, wall clock
+    ts.per_call(s.cuda_stream)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ts.per_call(s.cuda_stream)
+    torch.cuda.synchronize()
+    eager_ms = (time.perf_counter() - t0) * 1e3 / reps
+    identical = same(ts.snapshot(), ref)
+    gp = graph_of(lambda: ts.per_call(s.cuda_stream))
+    percall_graph_ms = time_graph(gp, reps)
+    nb = info["blocks"]
+    rec = {"textures": n_textures, "levels": sum(len(lv) for lv in ts.levels), "blocks": nb,
+           "batch_ms": round(batch_ms, 3), "batch_mblocks_s": round(nb / batch_ms / 1e3, 2),
+           "per_call_eager_ms": round(eager_ms, 3), "per_call_graph_ms": round(percall_graph_ms, 3),
+           "gain_vs_per_call_eager": round(eager_ms / batch_ms, 2),
+           "gain_vs_per_call_graph": round(percall_graph_ms / batch_ms, 2),
+           "identical_to_per_call": identical, "tuning": chosen.as_dict(),
+           "setup_s": {"generate_and_mips": round(gen_s, 2), "autotune": round(tune_s, 2)},
+           "launch": "one CUDA graph replay: counter memset + persistent lane kernel + persistent team kernel"}
+    b.close()
+    del ts, gb, gp
+    torch.cuda.empty_cache()
+    return rec
+
+
 def run_case(args):
     """One workload, device timing only (used for ncu captures)."""
     import torch
@@ -529,6 +601,12 @@ def main():
         return run_reference(args)
     if args.case:
         return run_case(args)
+    if args.batched_only:
+        import torch
+        import texpresso_gb300 as tx
+        torch.cuda.set_device(0)
+        print(json.dumps({"batched": batched(torch, tx, args)}), flush=True)
+        return 0
     return run_ours(args)
 
 

@@ -132,6 +132,78 @@ TX_API int tx_decompress_block(int format, const uint8_t *block, size_t block_le
 TX_API int tx_decompress_device(int format, const void *data, size_t data_len, size_t width,
                                 size_t height, void *output, size_t out_pitch, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Batched form (no counterpart in the reference, which compresses one image
+ * per call, lib/src/lib.rs:287): many textures / mip levels of mixed formats
+ * and algorithms in one stream-ordered launch.  Each item is compressed
+ * exactly as tx_compress_device would compress it. */
+
+/* One texture level in device memory. */
+typedef struct tx_batch_item {
+    const void *src;      /* width x height pixels of `channels` bytes */
+    size_t src_pitch;     /* bytes between rows */
+    uint32_t width, height;
+    int32_t format;       /* TX_FORMAT_* */
+    int32_t channels;     /* 4 = RGBA8; 1 = R8 (BC4); 2 = RG8 (BC5) */
+    tx_params params;
+    void *dst;            /* tx_compressed_size(format, width, height) bytes, block-size aligned */
+} tx_batch_item;
+
+/* Launch shape of the two persistent kernels.  Zero fields take defaults. */
+typedef struct tx_batch_tuning {
+    int32_t team_lanes;            /* lanes per ClusterFit block: 16 or 32 */
+    int32_t team_threads_per_cta;  /* threads per CTA of the ClusterFit kernel: 64..256 */
+    int32_t team_ctas_per_sm;      /* persistent grid = SMs x this */
+    int32_t team_blocks_per_unit;  /* ClusterFit blocks a team takes per queue pop */
+    int32_t lane_ctas_per_sm;      /* RangeFit/BC4/BC5 kernel: persistent grid = SMs x this */
+    int32_t lane_blocks_per_lane;  /* blocks per lane per queue pop (units of 32 x this) */
+} tx_batch_tuning;
+
+typedef struct tx_batch tx_batch;  /* opaque plan; not thread-safe */
+
+TX_API void tx_batch_default_tuning(tx_batch_tuning *tuning);
+
+/* Validate the items and build the plan (allocates device memory for the
+ * item table, the work queues and two counters).  Items are read at launch
+ * time, so their buffers must stay valid while the plan is launched. */
+TX_API int tx_batch_create(const tx_batch_item *items, size_t nitems, const tx_batch_tuning *tuning,
+                           tx_batch **batch);
+
+/* Enqueue the whole batch on `stream` (a memset of the queue counters and
+ * the persistent kernels, forked onto an internal second stream and joined
+ * back).  Capturable in a CUDA graph; do not launch one plan concurrently
+ * on two streams. */
+TX_API int tx_batch_launch(tx_batch *batch, void *stream);
+
+TX_API int tx_batch_set_tuning(tx_batch *batch, const tx_batch_tuning *tuning);
+TX_API int tx_batch_get_tuning(const tx_batch *batch, tx_batch_tuning *tuning);
+TX_API int tx_batch_info(const tx_batch *batch, size_t *nblocks, size_t *lane_units, size_t *team_units);
+
+/* Time candidate launch shapes on this batch (coordinate descent, `repeats`
+ * launches per candidate, CUDA events on `stream`), keep the fastest and
+ * return it in *chosen (may be NULL).  Synchronises `stream`. */
+TX_API int tx_batch_autotune(tx_batch *batch, void *stream, int repeats, tx_batch_tuning *chosen);
+
+TX_API void tx_batch_destroy(tx_batch *batch);
+
+/* Mip producer (the reference builds no mips, cli/src/main.rs:153): one level
+ * step, next = max(1, size / 2) per axis, each output channel the 2x2 box
+ * average (a+b+c+d+2)>>2 of the source with coordinates clamped at odd edges. */
+typedef struct tx_mip_job {
+    const void *src;
+    size_t src_pitch;
+    uint32_t width, height;  /* source level size */
+    int32_t channels;        /* bytes per pixel, 1..4 */
+    void *dst;
+    size_t dst_pitch;
+} tx_mip_job;
+
+/* Number of levels of a full chain down to 1x1 (0 for an empty image). */
+TX_API uint32_t tx_mip_count(uint32_t width, uint32_t height);
+
+/* Produce one level for every job, stream-ordered, no allocation. */
+TX_API int tx_mip_batch_device(const tx_mip_job *jobs, size_t njobs, void *stream);
+
 /* The CUDA error behind the last TX_ERR_CUDA returned on this thread
  * (a cudaError_t value), or 0. */
 TX_API int tx_last_cuda_error(void);

@@ -99,3 +99,26 @@ def test_no_cpu_fallback_without_device(tx):
     with pytest.raises(tx.TexpressoError) as e:
         tx.Format.Bc1.compress(bytes(64), 4, 4, tx.Params(), bytearray(8))
     assert e.value.status == -6
+
+
+def test_batch_rejects_bad_items_without_device(tx):
+    buf = np.zeros(1024, np.uint8)
+    ok = tx.batch_item(0, buf.ctypes.data, 16, 4, 4, tx.Params(), buf.ctypes.data)
+    bad_fmt = tx.batch_item(9, buf.ctypes.data, 16, 4, 4, tx.Params(), buf.ctypes.data)
+    bad_ch = tx.batch_item(0, buf.ctypes.data, 16, 4, 4, tx.Params(), buf.ctypes.data, channels=2)
+    bad_pitch = tx.batch_item(0, buf.ctypes.data, 8, 4, 4, tx.Params(), buf.ctypes.data)
+    bad_align = tx.batch_item(2, buf.ctypes.data, 16, 4, 4, tx.Params(), buf.ctypes.data + 8)
+    for item, status in ((bad_fmt, -1), (bad_ch, -2), (bad_pitch, -2), (bad_align, -9)):
+        with pytest.raises(tx.TexpressoError) as e:
+            tx.Batch([ok, item])
+        assert e.value.status == status
+    assert tx.mip_count(0, 5) == 0 and tx.mip_count(1, 1) == 1 and tx.mip_count(4096, 2) == 13
+
+
+def test_mip_reference_definition():
+    from texpresso_gb300 import workloads
+    img = np.arange(5 * 3 * 4, dtype=np.uint8).reshape(3, 5, 4)
+    m = workloads.mip_reference(img)
+    assert m.shape == (1, 2, 4)
+    a = img.astype(int)
+    assert m[0, 1, 0] == (a[0, 2, 0] + a[0, 3, 0] + a[1, 2, 0] + a[1, 3, 0] + 2) >> 2

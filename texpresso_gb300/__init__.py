@@ -214,3 +214,116 @@ def kernel_launch_count():
 def library():
     """The loaded ctypes library (for tests of the raw C ABI)."""
     return _lib
+
+
+# ---------------------------------------------------------------------------
+# batched form (tx_batch_*) and mip producer (tx_mip_*)
+
+class BatchItem(ctypes.Structure):
+    """tx_batch_item: one texture level in device memory."""
+    _fields_ = [("src", _vp), ("src_pitch", _sz), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("format", ctypes.c_int32), ("channels", ctypes.c_int32), ("params", _CParams), ("dst", _vp)]
+
+
+class BatchTuning(ctypes.Structure):
+    """tx_batch_tuning: launch shape of the persistent batch kernels."""
+    _fields_ = [("team_lanes", ctypes.c_int32), ("team_threads_per_cta", ctypes.c_int32),
+                ("team_ctas_per_sm", ctypes.c_int32), ("team_blocks_per_unit", ctypes.c_int32),
+                ("lane_ctas_per_sm", ctypes.c_int32), ("lane_blocks_per_lane", ctypes.c_int32)]
+
+    def as_dict(self):
+        return {f: int(getattr(self, f)) for f, _ in self._fields_}
+
+
+class MipJob(ctypes.Structure):
+    """tx_mip_job: one level step of one image in device memory."""
+    _fields_ = [("src", _vp), ("src_pitch", _sz), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32),
+                ("channels", ctypes.c_int32), ("dst", _vp), ("dst_pitch", _sz)]
+
+
+_lib.tx_batch_default_tuning.argtypes = [ctypes.POINTER(BatchTuning)]
+_lib.tx_batch_create.argtypes = [ctypes.POINTER(BatchItem), _sz, ctypes.POINTER(BatchTuning), ctypes.POINTER(_vp)]
+_lib.tx_batch_launch.argtypes = [_vp, _vp]
+_lib.tx_batch_set_tuning.argtypes = [_vp, ctypes.POINTER(BatchTuning)]
+_lib.tx_batch_get_tuning.argtypes = [_vp, ctypes.POINTER(BatchTuning)]
+_lib.tx_batch_info.argtypes = [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_sz), ctypes.POINTER(_sz)]
+_lib.tx_batch_autotune.argtypes = [_vp, _vp, ctypes.c_int, ctypes.POINTER(BatchTuning)]
+_lib.tx_batch_destroy.argtypes = [_vp]
+_lib.tx_batch_destroy.restype = None
+_lib.tx_mip_count.restype = ctypes.c_uint32
+_lib.tx_mip_count.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
+_lib.tx_mip_batch_device.argtypes = [ctypes.POINTER(MipJob), _sz, _vp]
+
+
+def batch_item(fmt, src_ptr, src_pitch, width, height, params, dst_ptr, channels=4):
+    it = BatchItem()
+    it.src, it.src_pitch, it.width, it.height = src_ptr, src_pitch, width, height
+    it.format, it.channels, it.params, it.dst = int(fmt), channels, params._c(), dst_ptr
+    return it
+
+
+class Batch:
+    """A plan over many texture levels, launched as one stream-ordered unit."""
+
+    def __init__(self, items, tuning=None):
+        arr = (BatchItem * max(1, len(items)))(*items)
+        self._items = arr
+        h = _vp()
+        _check(_lib.tx_batch_create(arr, len(items), ctypes.byref(tuning) if tuning else None, ctypes.byref(h)),
+               "tx_batch_create")
+        self._h = h
+
+    def launch(self, stream=0):
+        _check(_lib.tx_batch_launch(self._h, stream or None), "tx_batch_launch")
+
+    def autotune(self, stream=0, repeats=3):
+        t = BatchTuning()
+        _check(_lib.tx_batch_autotune(self._h, stream or None, repeats, ctypes.byref(t)), "tx_batch_autotune")
+        return t
+
+    @property
+    def tuning(self):
+        t = BatchTuning()
+        _check(_lib.tx_batch_get_tuning(self._h, ctypes.byref(t)), "tx_batch_get_tuning")
+        return t
+
+    @tuning.setter
+    def tuning(self, t):
+        _check(_lib.tx_batch_set_tuning(self._h, ctypes.byref(t)), "tx_batch_set_tuning")
+
+    def info(self):
+        nb, nl, nt = _sz(), _sz(), _sz()
+        _check(_lib.tx_batch_info(self._h, ctypes.byref(nb), ctypes.byref(nl), ctypes.byref(nt)), "tx_batch_info")
+        return {"blocks": nb.value, "lane_units": nl.value, "team_units": nt.value}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.tx_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def default_batch_tuning():
+    t = BatchTuning()
+    _lib.tx_batch_default_tuning(ctypes.byref(t))
+    return t
+
+
+def mip_count(width, height):
+    return int(_lib.tx_mip_count(width, height))
+
+
+def mip_batch_device(jobs, stream=0):
+    """One mip level step for every (src, pitch, w, h, channels, dst, dst_pitch) job."""
+    if not jobs:
+        return
+    arr = (MipJob * len(jobs))()
+    for i, (src, sp, w, h, ch, dst, dp) in enumerate(jobs):
+        arr[i].src, arr[i].src_pitch, arr[i].width, arr[i].height = src, sp, w, h
+        arr[i].channels, arr[i].dst, arr[i].dst_pitch = ch, dst, dp
+    _check(_lib.tx_mip_batch_device(arr, len(jobs), stream or None), "tx_mip_batch_device")

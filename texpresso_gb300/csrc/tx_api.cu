@@ -117,6 +117,7 @@ int ensure_ready(DeviceState **out) {
     build_single_table(6, 4, lut[3]);
     cudaError_t e = tx::upload_colour_tables(lut);
     if (e != cudaSuccess) return fail(e);
+    if ((e = tx::upload_batch_tables(lut)) != cudaSuccess) return fail(e);
     for (int s = 0; s < kStreams; ++s)
         if ((e = cudaStreamCreateWithFlags(&d.streams[s], cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
     if ((e = cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return fail(e);
@@ -177,6 +178,13 @@ int check_compress(int format, size_t width, size_t height, size_t output_len, s
 }
 
 }  // namespace
+
+int tx_internal_ensure_device() {
+    DeviceState *d = nullptr;
+    return ensure_ready(&d);
+}
+
+void tx_internal_set_last_cuda_error(int err) { t_last_cuda = err; }
 
 extern "C" {
 

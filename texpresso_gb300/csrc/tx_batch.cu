@@ -1,0 +1,542 @@
+// tx_batch.cu -- many textures (and their mip levels) in one stream-ordered,
+// CUDA-graph-capturable launch.
+//
+// A plan (tx_batch) holds, in device memory, one descriptor per texture level
+// and two work queues of "units" (a run of blocks of one level):
+//   lane units  RangeFit, BC4, BC5 -- thread-per-block code; a warp pops a unit
+//               of 32 x U blocks (U = blocks per lane) and each lane encodes
+//               every 32nd block of it;
+//   team units  ClusterFit, IterativeClusterFit -- a team of 32 lanes encodes
+//               the unit's C blocks one after another.
+// Each queue is drained by a persistent kernel (grid = SMs x CTAs per SM);
+// warps pop units with one atomicAdd on the queue's counter, so uneven levels
+// (4x4 mips next to 4096x4096 bases) balance themselves.  Team units are
+// ordered most expensive first (iterative before single-pass).  The two
+// kernels run on two streams forked from the caller's stream; a launch is a
+// memset of the counters plus the two kernels, so it can be captured in a
+// CUDA graph and replayed.
+//
+// The per-block code is the single-texture code (tx_colour.cuh,
+// tx_alpha.cuh), so a batch produces exactly the bytes of per-texture calls.
+#include "texpresso_gb300.h"
+#include "tx_alpha.cuh"
+#include "tx_colour.cuh"
+#include "tx_internal.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cstring>
+#include <new>
+#include <vector>
+
+namespace tx {
+
+enum UnitKind : int32_t { KIND_ALPHA = 0, KIND_RANGE = 1, KIND_CLUSTER = 2, KIND_CLUSTER_ITER = 3 };
+
+struct BatchItem {
+    SrcDesc src;
+    DevParams prm;
+    uint8_t *dst;
+    uint32_t nblocks;
+    int32_t format;
+    int32_t kind;
+    int32_t channels;
+};
+
+struct BatchQueue {
+    const BatchItem *items;
+    const uint2 *units;     // (item, first block)
+    uint32_t nunits;
+    uint32_t *counter;
+    uint32_t per_unit;      // lane units: blocks per lane; team units: blocks per unit
+};
+
+cudaError_t upload_batch_tables(const uint32_t lut[4][256][2]) { return upload_tables_this_tu(lut); }
+
+template <int TEAM>
+__global__ void __launch_bounds__(256) k_batch_teams(BatchQueue q) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    uint32_t *tbl = reinterpret_cast<uint32_t *>(smem_raw);
+    load_cand_tables(tbl);
+    TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw + kCandTblBytes);
+    __syncthreads();
+    const uint32_t *tbl4 = tbl, *tbl3 = tbl + kCand4 + 1;
+    const Team<TEAM> tm;
+    TeamSmem &sm = teams[threadIdx.x / TEAM];
+    for (;;) {
+        uint32_t u = 0;
+        if (tm.lane == 0) u = atomicAdd(q.counter, 1u);
+        u = tm.shfl(u, 0);
+        if (u >= q.nunits) break;
+        const uint2 unit = q.units[u];
+        const BatchItem &it = q.items[unit.x];
+        const SrcDesc src = it.src;
+        const DevParams prm = it.prm;
+        uint8_t *dst = it.dst;
+        const uint32_t end = min(unit.y + q.per_unit, it.nblocks);
+        const int sel = it.format * 2 + (it.kind == KIND_CLUSTER_ITER ? 1 : 0);
+        for (uint32_t b = unit.y; b < end; ++b) {
+            switch (sel) {
+            case BC1 * 2: cluster_block<BC1, TEAM, 1>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
+            case BC1 * 2 + 1: cluster_block<BC1, TEAM, 8>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
+            case BC2 * 2: cluster_block<BC2, TEAM, 1>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
+            case BC2 * 2 + 1: cluster_block<BC2, TEAM, 8>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
+            case BC3 * 2: cluster_block<BC3, TEAM, 1>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
+            case BC3 * 2 + 1: cluster_block<BC3, TEAM, 8>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
+            default: break;
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_batch_lanes(BatchQueue q) {
+    __shared__ float s_unorm[256];
+    __shared__ float s_sqrt[17];
+    init_unorm_tables(s_unorm, s_sqrt);
+    const int lane = threadIdx.x & 31;
+    for (;;) {
+        uint32_t u = 0;
+        if (lane == 0) u = atomicAdd(q.counter, 1u);
+        u = __shfl_sync(0xFFFFFFFFu, u, 0);
+        if (u >= q.nunits) break;
+        const uint2 unit = q.units[u];
+        const BatchItem &it = q.items[unit.x];
+        const SrcDesc src = it.src;
+        const DevParams prm = it.prm;
+        uint8_t *dst = it.dst;
+        const int kind = it.kind, fmt = it.format, ch = it.channels;
+        for (uint32_t k = 0; k < q.per_unit; ++k) {
+            const uint32_t b = unit.y + 32u * k + (uint32_t)lane;
+            if (b >= it.nblocks) break;
+            if (kind == KIND_RANGE) {
+                if (fmt == BC1) range_block<BC1>(src, b, prm, dst, s_unorm, s_sqrt);
+                else if (fmt == BC2) range_block<BC2>(src, b, prm, dst, s_unorm, s_sqrt);
+                else range_block<BC3>(src, b, prm, dst, s_unorm, s_sqrt);
+            } else if (fmt == BC4) {
+                if (ch == 1) alpha_block<BC4, 1>(src, b, dst);
+                else alpha_block<BC4, 4>(src, b, dst);
+            } else {
+                if (ch == 2) alpha_block<BC5, 2>(src, b, dst);
+                else alpha_block<BC5, 4>(src, b, dst);
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// mip producer: 2x2 box filter, (a+b+c+d+2)>>2 per channel, source
+// coordinates clamped at odd edges.  (The reference builds no mips,
+// cli/src/main.rs:153; this filter is the project's own definition.)
+
+struct MipJobDev {
+    const uint8_t *src;
+    uint8_t *dst;
+    uint32_t sw, sh, dw, dh;
+    uint32_t spitch, dpitch;
+    int32_t channels;
+};
+
+constexpr int kMipJobsPerLaunch = 256;  // 256 x 40 B of kernel parameters
+struct MipJobs {
+    MipJobDev job[kMipJobsPerLaunch];
+};
+
+__global__ void __launch_bounds__(256) k_mip(const __grid_constant__ MipJobs jobs, uint32_t njobs) {
+    const uint32_t j = blockIdx.y;
+    if (j >= njobs) return;
+    const MipJobDev job = jobs.job[j];
+    const uint32_t n = job.dw * job.dh;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const uint32_t x = i % job.dw, y = i / job.dw;
+        const uint32_t x0 = min(2 * x, job.sw - 1), x1 = min(2 * x + 1, job.sw - 1);
+        const uint32_t y0 = min(2 * y, job.sh - 1), y1 = min(2 * y + 1, job.sh - 1);
+        const uint8_t *r0 = job.src + (size_t)y0 * job.spitch, *r1 = job.src + (size_t)y1 * job.spitch;
+        uint8_t *d = job.dst + (size_t)y * job.dpitch + (size_t)x * job.channels;
+        for (int c = 0; c < job.channels; ++c) {
+            const uint32_t s = r0[x0 * job.channels + c] + r0[x1 * job.channels + c] + r1[x0 * job.channels + c] +
+                               r1[x1 * job.channels + c];
+            d[c] = (uint8_t)((s + 2) >> 2);
+        }
+    }
+}
+
+}  // namespace tx
+
+// ===========================================================================
+// C ABI
+
+struct tx_batch {
+    int device = 0;
+    std::vector<tx_batch_item> items;
+    std::vector<tx::BatchItem> desc;
+    tx::BatchItem *d_items = nullptr;
+    uint2 *d_lane_units = nullptr, *d_team_units = nullptr;
+    uint32_t *d_counters = nullptr;
+    uint32_t n_lane = 0, n_team = 0;
+    size_t nblocks = 0;
+    tx_batch_tuning tuning{};
+    cudaStream_t side = nullptr;
+    cudaEvent_t fork = nullptr, join = nullptr;
+    int sm_count = 0;
+};
+
+namespace {
+
+constexpr int kTeamMaxThreads = 256;  // __launch_bounds__ of k_batch_teams
+
+void default_tuning(tx_batch_tuning *t) {
+    t->team_lanes = 32;
+    t->team_threads_per_cta = 256;
+    t->team_ctas_per_sm = 4;
+    t->team_blocks_per_unit = 1;
+    t->lane_ctas_per_sm = 3;
+    t->lane_blocks_per_lane = 2;
+}
+
+void fill_tuning(const tx_batch_tuning *in, tx_batch_tuning *out) {
+    default_tuning(out);
+    if (!in) return;
+    if (in->team_lanes == 16 || in->team_lanes == 32) out->team_lanes = in->team_lanes;
+    if (in->team_threads_per_cta >= 64 && in->team_threads_per_cta <= kTeamMaxThreads &&
+        in->team_threads_per_cta % 32 == 0)
+        out->team_threads_per_cta = in->team_threads_per_cta;
+    if (in->team_ctas_per_sm >= 1 && in->team_ctas_per_sm <= 16) out->team_ctas_per_sm = in->team_ctas_per_sm;
+    if (in->team_blocks_per_unit >= 1 && in->team_blocks_per_unit <= 64) out->team_blocks_per_unit = in->team_blocks_per_unit;
+    if (in->lane_ctas_per_sm >= 1 && in->lane_ctas_per_sm <= 16) out->lane_ctas_per_sm = in->lane_ctas_per_sm;
+    if (in->lane_blocks_per_lane >= 1 && in->lane_blocks_per_lane <= 64) out->lane_blocks_per_lane = in->lane_blocks_per_lane;
+}
+
+int fail_batch(cudaError_t e) {
+    tx_internal_set_last_cuda_error((int)e);
+    return e == cudaErrorMemoryAllocation ? TX_ERR_OUT_OF_MEMORY : TX_ERR_CUDA;
+}
+
+// (Re)build the unit queues for the current tuning and upload them.
+int build_units(tx_batch *b) {
+    std::vector<uint2> lane, team_iter, team;
+    const uint32_t lane_span = 32u * (uint32_t)b->tuning.lane_blocks_per_lane;
+    const uint32_t team_span = (uint32_t)b->tuning.team_blocks_per_unit;
+    for (uint32_t i = 0; i < b->desc.size(); ++i) {
+        const tx::BatchItem &d = b->desc[i];
+        if (d.kind == tx::KIND_ALPHA || d.kind == tx::KIND_RANGE) {
+            for (uint32_t f = 0; f < d.nblocks; f += lane_span) lane.push_back(make_uint2(i, f));
+        } else {
+            auto &dst = d.kind == tx::KIND_CLUSTER_ITER ? team_iter : team;
+            for (uint32_t f = 0; f < d.nblocks; f += team_span) dst.push_back(make_uint2(i, f));
+        }
+    }
+    team_iter.insert(team_iter.end(), team.begin(), team.end());  // most expensive first
+    cudaFree(b->d_lane_units);
+    cudaFree(b->d_team_units);
+    b->d_lane_units = b->d_team_units = nullptr;
+    b->n_lane = (uint32_t)lane.size();
+    b->n_team = (uint32_t)team_iter.size();
+    cudaError_t e;
+    if (b->n_lane) {
+        if ((e = cudaMalloc(&b->d_lane_units, lane.size() * sizeof(uint2))) != cudaSuccess) return fail_batch(e);
+        if ((e = cudaMemcpy(b->d_lane_units, lane.data(), lane.size() * sizeof(uint2), cudaMemcpyHostToDevice)) != cudaSuccess)
+            return fail_batch(e);
+    }
+    if (b->n_team) {
+        if ((e = cudaMalloc(&b->d_team_units, team_iter.size() * sizeof(uint2))) != cudaSuccess) return fail_batch(e);
+        if ((e = cudaMemcpy(b->d_team_units, team_iter.data(), team_iter.size() * sizeof(uint2), cudaMemcpyHostToDevice)) !=
+            cudaSuccess)
+            return fail_batch(e);
+    }
+    return TX_OK;
+}
+
+template <int TEAM>
+cudaError_t launch_teams(tx_batch *b, cudaStream_t st) {
+    const int threads = b->tuning.team_threads_per_cta;
+    const size_t smem = tx::cluster_smem_bytes(TEAM, threads);
+    static bool attr_set[64][2] = {};
+    if (b->device < 64 && !attr_set[b->device][TEAM == 16]) {
+        cudaError_t e = cudaFuncSetAttribute(tx::k_batch_teams<TEAM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)tx::cluster_smem_bytes(TEAM, 1024));
+        if (e != cudaSuccess) return e;
+        attr_set[b->device][TEAM == 16] = true;
+    }
+    const uint32_t units_per_cta = (uint32_t)(threads / TEAM);
+    uint32_t grid = (uint32_t)(b->sm_count * b->tuning.team_ctas_per_sm);
+    const uint32_t need = (b->n_team + units_per_cta - 1) / units_per_cta;
+    if (grid > need) grid = need;
+    if (grid == 0) grid = 1;
+    tx::BatchQueue q{b->d_items, b->d_team_units, b->n_team, b->d_counters + 1,
+                     (uint32_t)b->tuning.team_blocks_per_unit};
+    tx::k_batch_teams<TEAM><<<grid, threads, smem, st>>>(q);
+    tx::note_launch();
+    return cudaGetLastError();
+}
+
+cudaError_t launch_lanes(tx_batch *b, cudaStream_t st) {
+    uint32_t grid = (uint32_t)(b->sm_count * b->tuning.lane_ctas_per_sm);
+    const uint32_t need = (b->n_lane + 3) / 4;  // 4 warps per CTA
+    if (grid > need) grid = need;
+    if (grid == 0) grid = 1;
+    tx::BatchQueue q{b->d_items, b->d_lane_units, b->n_lane, b->d_counters,
+                     (uint32_t)b->tuning.lane_blocks_per_lane};
+    tx::k_batch_lanes<<<grid, 128, 0, st>>>(q);
+    tx::note_launch();
+    return cudaGetLastError();
+}
+
+int launch_impl(tx_batch *b, cudaStream_t st) {
+    cudaError_t e;
+    if ((e = cudaMemsetAsync(b->d_counters, 0, 2 * sizeof(uint32_t), st)) != cudaSuccess) return fail_batch(e);
+    const bool both = b->n_lane && b->n_team;
+    if (both) {
+        if ((e = cudaEventRecord(b->fork, st)) != cudaSuccess) return fail_batch(e);
+        if ((e = cudaStreamWaitEvent(b->side, b->fork, 0)) != cudaSuccess) return fail_batch(e);
+    }
+    if (b->n_team) {
+        e = b->tuning.team_lanes == 16 ? launch_teams<16>(b, st) : launch_teams<32>(b, st);
+        if (e != cudaSuccess) return fail_batch(e);
+    }
+    if (b->n_lane) {
+        if ((e = launch_lanes(b, both ? b->side : st)) != cudaSuccess) return fail_batch(e);
+    }
+    if (both) {
+        if ((e = cudaEventRecord(b->join, b->side)) != cudaSuccess) return fail_batch(e);
+        if ((e = cudaStreamWaitEvent(st, b->join, 0)) != cudaSuccess) return fail_batch(e);
+    }
+    return TX_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+uint32_t tx_mip_count(uint32_t width, uint32_t height) {
+    if (width == 0 || height == 0) return 0;
+    uint32_t n = 1;
+    while (width > 1 || height > 1) {
+        width = width > 1 ? width >> 1 : 1;
+        height = height > 1 ? height >> 1 : 1;
+        ++n;
+    }
+    return n;
+}
+
+int tx_mip_batch_device(const tx_mip_job *jobs, size_t njobs, void *stream) {
+    if (njobs == 0) return TX_OK;
+    if (!jobs) return TX_ERR_INVALID_ARGUMENT;
+    for (size_t i = 0; i < njobs; ++i) {
+        const tx_mip_job &j = jobs[i];
+        if (!j.src || !j.dst || j.width == 0 || j.height == 0) return TX_ERR_INVALID_ARGUMENT;
+        if (j.channels < 1 || j.channels > 4) return TX_ERR_INVALID_ARGUMENT;
+        const uint32_t dw = j.width > 1 ? j.width >> 1 : 1, dh = j.height > 1 ? j.height >> 1 : 1;
+        if (j.src_pitch < (size_t)j.width * j.channels || j.dst_pitch < (size_t)dw * j.channels)
+            return TX_ERR_INVALID_ARGUMENT;
+        if (j.src_pitch > 0xFFFFFFFFu || j.dst_pitch > 0xFFFFFFFFu) return TX_ERR_INVALID_ARGUMENT;
+    }
+    int rc = tx_internal_ensure_device();
+    if (rc != TX_OK) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // jobs travel as kernel parameters: no allocation, no copy, capturable
+    for (size_t base = 0; base < njobs; base += tx::kMipJobsPerLaunch) {
+        const size_t n = std::min<size_t>(tx::kMipJobsPerLaunch, njobs - base);
+        tx::MipJobs pj;
+        std::memset(&pj, 0, sizeof(pj));
+        uint32_t maxpix = 0;
+        for (size_t i = 0; i < n; ++i) {
+            const tx_mip_job &j = jobs[base + i];
+            const uint32_t dw = j.width > 1 ? j.width >> 1 : 1, dh = j.height > 1 ? j.height >> 1 : 1;
+            pj.job[i] = tx::MipJobDev{static_cast<const uint8_t *>(j.src), static_cast<uint8_t *>(j.dst), j.width,
+                                      j.height, dw, dh, (uint32_t)j.src_pitch, (uint32_t)j.dst_pitch, j.channels};
+            maxpix = std::max(maxpix, dw * dh);
+        }
+        const uint32_t gx = std::min<uint32_t>((maxpix + 255) / 256, 1024);
+        tx::k_mip<<<dim3(gx, (unsigned)n), 256, 0, st>>>(pj, (uint32_t)n);
+        tx::note_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return fail_batch(e);
+    }
+    return TX_OK;
+}
+
+void tx_batch_default_tuning(tx_batch_tuning *t) {
+    if (t) default_tuning(t);
+}
+
+int tx_batch_create(const tx_batch_item *items, size_t nitems, const tx_batch_tuning *tuning, tx_batch **out) {
+    if (!out) return TX_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    if (nitems && !items) return TX_ERR_INVALID_ARGUMENT;
+    if (nitems > 0xFFFFFFFFu) return TX_ERR_INVALID_ARGUMENT;
+    // argument checks first (host only), then the device
+    for (size_t i = 0; i < nitems; ++i) {
+        const tx_batch_item &it = items[i];
+        const size_t bs = tx_block_size(it.format);
+        const bool ch_ok = it.channels == 4 || (it.channels == 1 && it.format == TX_FORMAT_BC4) ||
+                           (it.channels == 2 && it.format == TX_FORMAT_BC5);
+        const int alg = it.params.algorithm;
+        if (bs == 0) return TX_ERR_INVALID_FORMAT;
+        if (!ch_ok || alg < TX_RANGE_FIT || alg > TX_ITERATIVE_CLUSTER_FIT || it.width == 0 ||
+            it.src_pitch < (size_t)it.width * it.channels || (it.height && !it.src) || !it.dst)
+            return TX_ERR_INVALID_ARGUMENT;
+        if ((reinterpret_cast<uintptr_t>(it.dst) % bs) != 0) return TX_ERR_MISALIGNED;
+        if (tx_num_blocks(it.width) * tx_num_blocks(it.height) > 0xFFFFFFF0u) return TX_ERR_INVALID_ARGUMENT;
+    }
+    int rc = tx_internal_ensure_device();
+    if (rc != TX_OK) return rc;
+    tx_batch *b = new (std::nothrow) tx_batch();
+    if (!b) return TX_ERR_OUT_OF_MEMORY;
+    cudaGetDevice(&b->device);
+    cudaDeviceGetAttribute(&b->sm_count, cudaDevAttrMultiProcessorCount, b->device);
+    fill_tuning(tuning, &b->tuning);
+    b->items.assign(items, items + nitems);
+    b->desc.resize(nitems);
+    for (size_t i = 0; i < nitems; ++i) {
+        const tx_batch_item &it = items[i];
+        tx::BatchItem &d = b->desc[i];
+        std::memset(&d, 0, sizeof(d));
+        const int f = it.format;
+        const int alg = it.params.algorithm;
+        const size_t nb = tx_num_blocks(it.width) * tx_num_blocks(it.height);
+        d.src.base = static_cast<const uint8_t *>(it.src);
+        d.src.masks = nullptr;
+        d.src.pitch = it.src_pitch;
+        d.src.width = it.width;
+        d.src.height = it.height;
+        d.src.blocks_wide = (uint32_t)tx_num_blocks(it.width);
+        d.src.channels = it.channels;
+        const size_t va = it.channels == 4 ? 16 : (size_t)it.channels * 4;
+        d.src.vec16 = ((reinterpret_cast<uintptr_t>(it.src) % va) == 0 && (it.src_pitch % va) == 0) ? 1 : 0;
+        d.src.mode = 0;
+        for (int c = 0; c < 3; ++c) d.prm.w[c] = it.params.weights[c];
+        d.prm.alpha_weighted = it.params.weigh_colour_by_alpha ? 1 : 0;
+        d.dst = static_cast<uint8_t *>(it.dst);
+        d.nblocks = (uint32_t)nb;
+        d.format = f;
+        d.channels = it.channels;
+        if (f == TX_FORMAT_BC4 || f == TX_FORMAT_BC5) d.kind = tx::KIND_ALPHA;
+        else if (alg == TX_RANGE_FIT) d.kind = tx::KIND_RANGE;
+        else d.kind = alg == TX_ITERATIVE_CLUSTER_FIT ? tx::KIND_CLUSTER_ITER : tx::KIND_CLUSTER;
+        b->nblocks += nb;
+    }
+    cudaError_t e;
+    if (nitems) {
+        if ((e = cudaMalloc(&b->d_items, nitems * sizeof(tx::BatchItem))) != cudaSuccess) { tx_batch_destroy(b); return fail_batch(e); }
+        if ((e = cudaMemcpy(b->d_items, b->desc.data(), nitems * sizeof(tx::BatchItem), cudaMemcpyHostToDevice)) != cudaSuccess) {
+            tx_batch_destroy(b);
+            return fail_batch(e);
+        }
+    }
+    if ((e = cudaMalloc(&b->d_counters, 2 * sizeof(uint32_t))) != cudaSuccess) { tx_batch_destroy(b); return fail_batch(e); }
+    if ((e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess ||
+        (e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming)) != cudaSuccess) {
+        tx_batch_destroy(b);
+        return fail_batch(e);
+    }
+    if ((rc = build_units(b)) != TX_OK) { tx_batch_destroy(b); return rc; }
+    *out = b;
+    return TX_OK;
+}
+
+int tx_batch_launch(tx_batch *b, void *stream) {
+    if (!b) return TX_ERR_INVALID_ARGUMENT;
+    return launch_impl(b, static_cast<cudaStream_t>(stream));
+}
+
+int tx_batch_set_tuning(tx_batch *b, const tx_batch_tuning *tuning) {
+    if (!b || !tuning) return TX_ERR_INVALID_ARGUMENT;
+    tx_batch_tuning t;
+    fill_tuning(tuning, &t);
+    const bool rebuild = t.team_blocks_per_unit != b->tuning.team_blocks_per_unit ||
+                         t.lane_blocks_per_lane != b->tuning.lane_blocks_per_lane;
+    b->tuning = t;
+    return rebuild ? build_units(b) : TX_OK;
+}
+
+int tx_batch_get_tuning(const tx_batch *b, tx_batch_tuning *tuning) {
+    if (!b || !tuning) return TX_ERR_INVALID_ARGUMENT;
+    *tuning = b->tuning;
+    return TX_OK;
+}
+
+int tx_batch_info(const tx_batch *b, size_t *nblocks, size_t *lane_units, size_t *team_units) {
+    if (!b) return TX_ERR_INVALID_ARGUMENT;
+    if (nblocks) *nblocks = b->nblocks;
+    if (lane_units) *lane_units = b->n_lane;
+    if (team_units) *team_units = b->n_team;
+    return TX_OK;
+}
+
+// Project-written autotuner: coordinate descent over the launch shape, each
+// candidate timed with CUDA events over `repeats` launches of this batch.
+int tx_batch_autotune(tx_batch *b, void *stream, int repeats, tx_batch_tuning *chosen) {
+    if (!b) return TX_ERR_INVALID_ARGUMENT;
+    if (repeats < 1) repeats = 1;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    cudaEvent_t e0, e1;
+    cudaError_t e;
+    if ((e = cudaEventCreate(&e0)) != cudaSuccess) return fail_batch(e);
+    if ((e = cudaEventCreate(&e1)) != cudaSuccess) { cudaEventDestroy(e0); return fail_batch(e); }
+    int rc = TX_OK;
+    auto measure = [&](const tx_batch_tuning &t, float *ms) -> int {
+        int r = tx_batch_set_tuning(b, &t);
+        if (r != TX_OK) return r;
+        if ((r = launch_impl(b, st)) != TX_OK) return r;  // warm
+        cudaEventRecord(e0, st);
+        for (int i = 0; i < repeats; ++i)
+            if ((r = launch_impl(b, st)) != TX_OK) return r;
+        cudaEventRecord(e1, st);
+        cudaError_t ee = cudaEventSynchronize(e1);
+        if (ee != cudaSuccess) return fail_batch(ee);
+        cudaEventElapsedTime(ms, e0, e1);
+        return TX_OK;
+    };
+    tx_batch_tuning best = b->tuning;
+    float best_ms = 0;
+    if ((rc = measure(best, &best_ms)) == TX_OK) {
+        struct Axis {
+            int32_t tx_batch_tuning::*field;
+            int opts[6];
+            int n;
+            bool team;
+        };
+        const Axis axes[] = {
+            {&tx_batch_tuning::team_lanes, {32, 16}, 2, true},
+            {&tx_batch_tuning::team_threads_per_cta, {64, 128, 256}, 3, true},
+            {&tx_batch_tuning::team_ctas_per_sm, {1, 2, 3, 4, 6, 8}, 6, true},
+            {&tx_batch_tuning::team_blocks_per_unit, {1, 2, 4, 8}, 4, true},
+            {&tx_batch_tuning::lane_ctas_per_sm, {2, 3, 4, 6}, 4, false},
+            {&tx_batch_tuning::lane_blocks_per_lane, {1, 2, 4, 8}, 4, false},
+        };
+        for (int pass = 0; pass < 2 && rc == TX_OK; ++pass) {
+            for (const Axis &ax : axes) {
+                if ((ax.team && !b->n_team) || (!ax.team && !b->n_lane)) continue;
+                for (int i = 0; i < ax.n && rc == TX_OK; ++i) {
+                    tx_batch_tuning t = best;
+                    if (t.*ax.field == ax.opts[i]) continue;
+                    t.*ax.field = ax.opts[i];
+                    float ms = 0;
+                    rc = measure(t, &ms);
+                    if (rc == TX_OK && ms < best_ms) { best_ms = ms; best = t; }
+                }
+            }
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != TX_OK) return rc;
+    rc = tx_batch_set_tuning(b, &best);
+    if (chosen) *chosen = best;
+    return rc;
+}
+
+void tx_batch_destroy(tx_batch *b) {
+    if (!b) return;
+    cudaFree(b->d_items);
+    cudaFree(b->d_lane_units);
+    cudaFree(b->d_team_units);
+    cudaFree(b->d_counters);
+    if (b->side) cudaStreamDestroy(b->side);
+    if (b->fork) cudaEventDestroy(b->fork);
+    if (b->join) cudaEventDestroy(b->join);
+    delete b;
+}
+
+}  // extern "C"

@@ -1,0 +1,807 @@
+// tx_colour.cuh -- per-block device code for BC1/BC2/BC3 colour endpoints and
+// the BC2/BC3 alpha halves, shared by the single-texture kernels (tx_colour.cu)
+// and the persistent batch kernel (tx_batch.cu).
+//
+// Two execution shapes:
+//   thread-per-block  ColourSet, SingleColourFit and RangeFit are short and
+//                     branch-light; a thread owns a block and 32 neighbouring
+//                     blocks load as four coalesced 512-byte rows.
+//   team-per-block    ClusterFit: a team of TEAM lanes (16 or 32) owns a block.
+//                     Lane p owns pixel p for ColourSet; the candidate sweep
+//                     (967 least-squares fits at 16 colours) is spread over the
+//                     team and reduced lexicographically on (error, position in
+//                     the reference's loop order), which selects exactly the
+//                     candidate the sequential "first strictly smaller error"
+//                     loop selects.
+// Both reproduce the reference's f32 operation order (see tx_device.cuh).
+// The constant tables are TU-local: every translation unit that includes this
+// header uploads its own copy with upload_tables_this_tu().
+#pragma once
+#include "tx_device.cuh"
+
+namespace tx {
+
+// Single-colour tables (lib/src/colourfit/single_lut.rs): [table][target][index]
+// packed start | end << 8 | error << 16.  Tables: 0 = 5_3, 1 = 6_3, 2 = 5_4, 3 = 6_4.
+static __constant__ uint32_t c_lut[4][256][2];
+
+// ClusterFit candidate lists.  Entry bits: 0-3 i (offset of S(0,i)),
+// 4-11 offset of S(i,j), 12-19 offset of S(j,k) (compress4 only),
+// 20-29 rank of (i,j[,k]) in the reference's loop order at 16 colours.
+// Entries are sorted so that the first N[n] are exactly the candidates of an
+// n-colour set (those with max(i+1, j, k) <= n).
+constexpr int kCand4 = 967, kCand3 = 151;
+static __device__ uint32_t g_cand[kCand4 + 1 + kCand3 + 1];
+static __constant__ uint32_t c_ncand4[17];
+static __constant__ uint32_t c_ncand3[17];
+
+// Row offsets of the packed triangular partial-sum table S(a,b), a <= b <= 16.
+__host__ __device__ constexpr int tri_off(int a) { return 17 * a - (a * (a - 1)) / 2; }
+__host__ __device__ constexpr int tri_idx(int a, int b) { return tri_off(a) + (b - a); }
+constexpr int kTri = 153;
+
+// ===========================================================================
+// Shared pieces
+
+struct Single {
+    uint32_t err;
+    float s[3], e[3];
+    uint32_t index;  // 0 or 2
+};
+
+// SingleColourFit::compute_endpoints (single.rs:58-106).
+__device__ __forceinline__ Single single_endpoints(const int (&col)[3], int t0, int t1, int t2) {
+    Single r;
+    r.err = 0xFFFFFFFFu;
+    r.index = 0;
+    r.s[0] = r.s[1] = r.s[2] = 0.0f;
+    r.e[0] = r.e[1] = r.e[2] = 0.0f;
+    const int tb[3] = {t0, t1, t2};
+#pragma unroll
+    for (int index = 0; index < 2; ++index) {
+        uint32_t src[3], err = 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            src[c] = c_lut[tb[c]][col[c]][index];
+            const uint32_t d = (src[c] >> 16) & 0xFFu;
+            err += d * d;
+        }
+        if (err < r.err) {
+            r.s[0] = div_rn((float)(src[0] & 0xFFu), 31.0f);
+            r.s[1] = div_rn((float)(src[1] & 0xFFu), 63.0f);
+            r.s[2] = div_rn((float)(src[2] & 0xFFu), 31.0f);
+            r.e[0] = div_rn((float)((src[0] >> 8) & 0xFFu), 31.0f);
+            r.e[1] = div_rn((float)((src[1] >> 8) & 0xFFu), 63.0f);
+            r.e[2] = div_rn((float)((src[2] >> 8) & 0xFFu), 31.0f);
+            r.index = 2u * (uint32_t)index;
+            r.err = err;
+        }
+    }
+    return r;
+}
+
+// 2-bit index word for "every valid pixel takes `index`, excluded pixels 3".
+__device__ __forceinline__ uint32_t uniform_indices(uint32_t valid16, uint32_t index) {
+    uint32_t w = 0;
+#pragma unroll
+    for (int p = 0; p < 16; ++p) w |= (((valid16 >> p) & 1u) ? index : 3u) << (2 * p);
+    return w;
+}
+
+// SingleColourFit + ColourFit::compress (colourfit.rs:44-60) given the colour.
+template <int FMT>
+__device__ __forceinline__ uint2 single_fit(const int (&col)[3], uint32_t valid16, bool transparent) {
+    uint32_t best_err = 0xFFFFFFFFu;
+    uint2 best = make_uint2(0u, 0u);
+    if (FMT == BC1) {
+        const Single f = single_endpoints(col, 0, 1, 0);  // LOOKUP_5_3, 6_3, 5_3
+        if (f.err < best_err) {
+            best = write3(pack_565(f.s[0], f.s[1], f.s[2]), pack_565(f.e[0], f.e[1], f.e[2]),
+                          uniform_indices(valid16, f.index));
+            best_err = f.err;
+        }
+    }
+    if (FMT != BC1 || !transparent) {
+        const Single f = single_endpoints(col, 2, 3, 2);  // LOOKUP_5_4, 6_4, 5_4
+        if (f.err < best_err) {
+            best = write4(pack_565(f.s[0], f.s[1], f.s[2]), pack_565(f.e[0], f.e[1], f.e[2]),
+                          uniform_indices(valid16, f.index));
+        }
+    }
+    return best;
+}
+
+// Sym3x3::principle_component (math.rs:75-97); only lanes x,y,z matter.
+__device__ __forceinline__ void principle_component(const float (&m)[6], float (&v)[3]) {
+    float vx = 1.0f, vy = 1.0f, vz = 1.0f;
+#pragma unroll 1
+    for (int it = 0; it < 8; ++it) {
+        float wx = m[0] * vx, wy = m[1] * vx, wz = m[2] * vx;
+        wx = m[1] * vy + wx; wy = m[3] * vy + wy; wz = m[4] * vy + wz;
+        wx = m[2] * vz + wx; wy = m[4] * vz + wy; wz = m[5] * vz + wz;
+        const float a = fmaxf(wx, fmaxf(wy, wz));
+        const float r = rcp_rn(a);
+        vx = wx * r; vy = wy * r; vz = wz * r;
+    }
+    v[0] = vx; v[1] = vy; v[2] = vz;
+}
+
+// Clamp to [0,1] and snap to the 5:6:5 grid (range.rs:87-98, cluster.rs:206-210).
+__device__ __forceinline__ float snap(float x, float grid, float gridrcp) {
+    x = fminf(1.0f, fmaxf(0.0f, x));
+    return truncf(grid * x + 0.5f) * gridrcp;
+}
+
+__device__ __forceinline__ uint32_t u8_of(uint32_t px, int c) { return (px >> (8 * c)) & 0xFFu; }
+
+// ===========================================================================
+// k_range: one thread per block
+
+template <int FMT>
+__device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], uint32_t inb,
+                                                     const DevParams &prm, const float *s_unorm,
+                                                     const float *s_sqrt) {
+    // ColourSet (colourset.rs:35-112), pixel-indexed: a "point" is the first
+    // pixel of its colour, and pixel order is point order.
+    uint32_t tbits = 0;
+    if (FMT == BC1) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) tbits |= ((px[i] >> 31) ^ 1u) << i;
+        tbits &= inb;
+    }
+    const uint32_t valid = inb & ~tbits;
+    const bool transparent = tbits != 0;
+    uint32_t key[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) key[i] = ((valid >> i) & 1u) ? (px[i] & 0xFFFFFFu) : (0x01000000u | (uint32_t)i);
+    int rep[16];
+    uint32_t newbits = 0;
+    uint64_t dupc = 0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        int r = i;
+#pragma unroll
+        for (int j = i - 1; j >= 0; --j) r = (key[j] == key[i]) ? j : r;
+        rep[i] = r;
+        if ((valid >> i) & 1u) {
+            if (r == i) newbits |= 1u << i;
+            else dupc += 1ull << (4 * r);
+        }
+    }
+    const int count = __popc(newbits);
+
+    if (count == 1) {
+        uint32_t rgb = 0;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) rgb |= ((valid >> i) & 1u) ? (px[i] & 0xFFFFFFu) : 0u;
+        int col[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) col[c] = f32_to_i32_clamped(s_unorm[u8_of(rgb, c)] * 255.0f, 255);
+        return single_fit<FMT>(col, valid, transparent);
+    }
+    float x[16], y[16], z[16], w[16];
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        x[i] = s_unorm[u8_of(px[i], 0)];
+        y[i] = s_unorm[u8_of(px[i], 1)];
+        z[i] = s_unorm[u8_of(px[i], 2)];
+    }
+    if (!prm.alpha_weighted) {
+#pragma unroll
+        for (int i = 0; i < 16; ++i) w[i] = s_sqrt[1 + (int)((dupc >> (4 * i)) & 0xFu)];
+    } else {
+        float wa[16];
+#pragma unroll
+        for (int i = 0; i < 16; ++i) wa[i] = (float)((px[i] >> 24) + 1u) * (1.0f / 256.0f);
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int i = j; i < 16; ++i) acc = acc + ((((valid >> i) & 1u) && rep[i] == j) ? wa[i] : 0.0f);
+            w[j] = sqrt_rn(acc);
+        }
+    }
+
+    // Sym3x3::weighted_covariance (math.rs:44-73)
+    float total = 0.0f, cx = 0.0f, cy = 0.0f, cz = 0.0f;
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+        if ((newbits >> i) & 1u) total = total + w[i];
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+        if ((newbits >> i) & 1u) { cx = cx + x[i] * w[i]; cy = cy + y[i] * w[i]; cz = cz + z[i] * w[i]; }
+    if (total > FLT_EPSILON) { cx = div_rn(cx, total); cy = div_rn(cy, total); cz = div_rn(cz, total); }
+    float m[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        if ((newbits >> i) & 1u) {
+            const float ax = x[i] - cx, ay = y[i] - cy, az = z[i] - cz;
+            const float bx = ax * w[i], by = ay * w[i], bz = az * w[i];
+            m[0] += ax * bx; m[1] += ax * by; m[2] += ax * bz;
+            m[3] += ay * by; m[4] += ay * bz; m[5] += az * bz;
+        }
+    }
+    float axis[3];
+    principle_component(m, axis);
+
+    // RangeFit::new (range.rs:44-101)
+    float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, e0 = 0.0f, e1 = 0.0f, e2 = 0.0f;
+    {
+        bool seen = false;
+        float mn = 0.0f, mx = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            if ((newbits >> i) & 1u) {
+                const float d = x[i] * axis[0] + y[i] * axis[1] + z[i] * axis[2];
+                if (!seen) { s0 = e0 = x[i]; s1 = e1 = y[i]; s2 = e2 = z[i]; mn = mx = d; seen = true; }
+                else if (d < mn) { s0 = x[i]; s1 = y[i]; s2 = z[i]; mn = d; }
+                else if (d > mx) { e0 = x[i]; e1 = y[i]; e2 = z[i]; mx = d; }
+            }
+        }
+    }
+    s0 = snap(s0, 31.0f, 1.0f / 31.0f); s1 = snap(s1, 63.0f, 1.0f / 63.0f); s2 = snap(s2, 31.0f, 1.0f / 31.0f);
+    e0 = snap(e0, 31.0f, 1.0f / 31.0f); e1 = snap(e1, 63.0f, 1.0f / 63.0f); e2 = snap(e2, 31.0f, 1.0f / 31.0f);
+
+    const float w0 = prm.w[0], w1 = prm.w[1], w2 = prm.w[2];
+    float best_err = FLT_MAX;
+    uint2 best = make_uint2(0u, 0u);
+
+    // compression_helper (range.rs:103-143) over a codebook of NC codes
+    auto helper = [&](const float (&cr)[4], const float (&cg)[4], const float (&cb)[4], int nc,
+                      uint32_t &indices) -> bool {
+        uint32_t closest = 0;
+        float err = 0.0f;
+#pragma unroll
+        for (int i = 0; i < 16; ++i) {
+            if ((newbits >> i) & 1u) {
+                float dist = FLT_MAX;
+                uint32_t idx = 0;
+#pragma unroll
+                for (int j = 0; j < 4; ++j) {
+                    if (j < nc) {
+                        const float dx = w0 * (x[i] - cr[j]), dy = w1 * (y[i] - cg[j]), dz = w2 * (z[i] - cb[j]);
+                        const float d = dx * dx + dy * dy + dz * dz;
+                        if (d < dist) { dist = d; idx = (uint32_t)j; }
+                    }
+                }
+                closest |= idx << (2 * i);
+                err += dist;
+            }
+        }
+        if (err < best_err) {
+            uint32_t out = 0;
+#pragma unroll
+            for (int p = 0; p < 16; ++p) {
+                const uint32_t v = ((valid >> p) & 1u) ? ((closest >> (2 * rep[p])) & 3u) : 3u;
+                out |= v << (2 * p);
+            }
+            indices = out;
+            best_err = err;
+            return true;
+        }
+        return false;
+    };
+
+    const uint32_t a565 = pack_565(s0, s1, s2), b565 = pack_565(e0, e1, e2);
+    if (FMT == BC1) {
+        const float cr[4] = {s0, e0, s0 * 0.5f + e0 * 0.5f, 0.0f};
+        const float cg[4] = {s1, e1, s1 * 0.5f + e1 * 0.5f, 0.0f};
+        const float cb[4] = {s2, e2, s2 * 0.5f + e2 * 0.5f, 0.0f};
+        uint32_t idx;
+        if (helper(cr, cg, cb, 3, idx)) best = write3(a565, b565, idx);
+    }
+    if (FMT != BC1 || !transparent) {
+        const float c23 = 2.0f / 3.0f, c13 = 1.0f / 3.0f;
+        const float cr[4] = {s0, e0, s0 * c23 + e0 * c13, s0 * c13 + e0 * c23};
+        const float cg[4] = {s1, e1, s1 * c23 + e1 * c13, s1 * c13 + e1 * c23};
+        const float cb[4] = {s2, e2, s2 * c23 + e2 * c13, s2 * c13 + e2 * c23};
+        uint32_t idx;
+        if (helper(cr, cg, cb, 4, idx)) best = write4(a565, b565, idx);
+    }
+    return best;
+}
+
+__device__ __forceinline__ void init_unorm_tables(float *s_unorm, float *s_sqrt) {
+    for (int i = threadIdx.x; i < 256; i += blockDim.x) s_unorm[i] = unorm8((uint32_t)i);
+    if (threadIdx.x < 17) s_sqrt[threadIdx.x] = sqrt_rn((float)threadIdx.x);
+    __syncthreads();
+}
+
+// ===========================================================================
+// k_cluster: one team per block
+
+template <int TEAM>
+struct Team {
+    unsigned mask;
+    int lane;
+    int base;
+    __device__ __forceinline__ Team() {
+        const int wl = threadIdx.x & 31;
+        lane = wl & (TEAM - 1);
+        base = wl & ~(TEAM - 1);
+        mask = (TEAM == 32) ? 0xFFFFFFFFu : (0xFFFFu << base);
+    }
+    __device__ __forceinline__ unsigned ballot(bool p) const {
+        const unsigned b = __ballot_sync(mask, p);
+        return (TEAM == 32) ? b : ((b >> base) & 0xFFFFu);
+    }
+    __device__ __forceinline__ bool all(bool p) const { return __all_sync(mask, p); }
+    template <class T> __device__ __forceinline__ T shfl(T v, int src) const { return __shfl_sync(mask, v, src, TEAM); }
+    template <class T> __device__ __forceinline__ T shfl_xor(T v, int m) const { return __shfl_xor_sync(mask, v, m, TEAM); }
+    __device__ __forceinline__ void sync() const { __syncwarp(mask); }
+    __device__ __forceinline__ unsigned match(uint32_t key) const {
+        const unsigned m = __match_any_sync(mask, key);
+        return (TEAM == 32) ? m : ((m >> base) & 0xFFFFu);
+    }
+};
+
+struct __align__(16) TeamSmem {
+    float4 S[kTri + 3];     // S(a,b) running sums, packed triangle (+pad)
+    float4 PW[16];          // points_weights in the current ordering
+    float P[4][16];         // x, y, z, weight of each point, point order
+    float D[16];            // dot products
+    uint32_t hist[8][4];    // orderings of earlier iterations (16 bytes each)
+};
+
+// fcmp of cluster.rs:90-97 as "a sorts before b" / "a and b tie".
+__device__ __forceinline__ bool dps_less(float a, float b) {
+    const bool fa = isfinite(a), fb = isfinite(b);
+    return fa && (!fb || a < b);
+}
+__device__ __forceinline__ bool dps_equiv(float a, float b) {
+    const bool fa = isfinite(a), fb = isfinite(b);
+    return (!fa && !fb) || (fa && fb && a == b);
+}
+
+__device__ __forceinline__ uint8_t hist_get(const TeamSmem &sm, int it, int m) {
+    return reinterpret_cast<const uint8_t *>(sm.hist[it])[m];
+}
+
+// One compress4 candidate (cluster.rs:320-353).  Returns the error, writes
+// the snapped endpoints when WANT_AB.
+template <bool WANT_AB>
+__device__ __forceinline__ float eval4(const float4 p0, const float4 p1, const float4 p2, const float4 xs,
+                                       const float (&cw)[3], float (&ea)[3], float (&eb)[3]) {
+    const float c13 = 1.0f / 3.0f, c19 = 1.0f / 9.0f, c23 = 2.0f / 3.0f, c49 = 4.0f / 9.0f, c29 = 2.0f / 9.0f;
+    const float p3x = xs.x - p2.x - p1.x - p0.x;
+    const float p3y = xs.y - p2.y - p1.y - p0.y;
+    const float p3z = xs.z - p2.z - p1.z - p0.z;
+    const float p3w = xs.w - p2.w - p1.w - p0.w;
+    const float ax[3] = {p2.x * c13 + (p1.x * c23 + p0.x), p2.y * c13 + (p1.y * c23 + p0.y),
+                         p2.z * c13 + (p1.z * c23 + p0.z)};
+    const float alpha2 = p2.w * c19 + (p1.w * c49 + p0.w);
+    const float bx[3] = {p1.x * c13 + (p2.x * c23 + p3x), p1.y * c13 + (p2.y * c23 + p3y),
+                         p1.z * c13 + (p2.z * c23 + p3z)};
+    const float beta2 = p1.w * c19 + (p2.w * c49 + p3w);
+    const float ab = c29 * (p1.w + p2.w);
+    const float factor = rcp_rn((alpha2 * beta2) - ab * ab);
+    const float grid[3] = {31.0f, 63.0f, 31.0f};
+    const float gridrcp[3] = {1.0f / 31.0f, 1.0f / 63.0f, 1.0f / 31.0f};
+    float e5[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float a = snap(((ax[c] * beta2) - bx[c] * ab) * factor, grid[c], gridrcp[c]);
+        const float b = snap(((bx[c] * alpha2) - ax[c] * ab) * factor, grid[c], gridrcp[c]);
+        const float e1 = (a * a) * alpha2 + (b * b * beta2);
+        const float e2 = (a * b * ab) - a * ax[c];
+        const float e3 = e2 - b * bx[c];
+        const float e4 = 2.0f * e3 + e1;
+        e5[c] = e4 * cw[c];
+        if (WANT_AB) { ea[c] = a; eb[c] = b; }
+    }
+    return e5[0] + e5[1] + e5[2];
+}
+
+// One compress3 candidate (cluster.rs:189-220).
+template <bool WANT_AB>
+__device__ __forceinline__ float eval3(const float4 p0, const float4 p1, const float4 xs, const float (&cw)[3],
+                                       float (&ea)[3], float (&eb)[3]) {
+    const float p2x = xs.x - p1.x - p0.x, p2y = xs.y - p1.y - p0.y, p2z = xs.z - p1.z - p0.z,
+                p2w = xs.w - p1.w - p0.w;
+    const float tx = p1.x * 0.5f, ty = p1.y * 0.5f, tz = p1.z * 0.5f, tw = p1.w * 0.25f;
+    const float ax[3] = {tx + p0.x, ty + p0.y, tz + p0.z};
+    const float alpha2 = tw + p0.w;
+    const float bx[3] = {tx + p2x, ty + p2y, tz + p2z};
+    const float beta2 = tw + p2w;
+    const float ab = tw;
+    const float factor = rcp_rn((alpha2 * beta2) - ab * ab);
+    const float grid[3] = {31.0f, 63.0f, 31.0f};
+    const float gridrcp[3] = {1.0f / 31.0f, 1.0f / 63.0f, 1.0f / 31.0f};
+    float e5[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float a = snap(((ax[c] * beta2) - bx[c] * ab) * factor, grid[c], gridrcp[c]);
+        const float b = snap(((bx[c] * alpha2) - ax[c] * ab) * factor, grid[c], gridrcp[c]);
+        const float e1 = (a * a) * alpha2 + (b * b * beta2);
+        const float e2 = (a * b * ab) - a * ax[c];
+        const float e3 = e2 - b * bx[c];
+        const float e4 = 2.0f * e3 + e1;
+        e5[c] = e4 * cw[c];
+        if (WANT_AB) { ea[c] = a; eb[c] = b; }
+    }
+    return e5[0] + e5[1] + e5[2];
+}
+
+// Decode (i, j, k) from a candidate entry.
+__device__ __forceinline__ void decode_entry(uint32_t e, int &i, int &j, int &k) {
+    i = (int)(e & 0xFu);
+    j = (int)((e >> 4) & 0xFFu) - tri_off(i) + i;
+    k = (int)((e >> 12) & 0xFFu) - tri_off(j) + j;
+}
+
+// ClusterFit::compress3 / compress4 (cluster.rs:152-417) for one team.
+// best_err / best carry the ColourFit state across compress3 -> compress4.
+template <int NC, int TEAM, int NITER>
+__device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm, const uint32_t *tbl, int count,
+                                             const float (&principal)[3], const float (&cw)[3], bool valid,
+                                             int my_point, float &best_err, uint2 &best) {
+    const int lane = tm.lane;
+    float run = best_err;
+    float ba[3] = {0.0f, 0.0f, 0.0f}, bb[3] = {0.0f, 0.0f, 0.0f};
+    uint32_t bentry = 0;
+    int bit = 0;
+    float axis[3] = {principal[0], principal[1], principal[2]};
+    const uint32_t ncand = (NC == 4) ? c_ncand4[count] : c_ncand3[count];
+    float4 xs = make_float4(0.f, 0.f, 0.f, 0.f);
+
+#pragma unroll 1
+    for (int it = 0; it < NITER; ++it) {
+        // construct_ordering (cluster.rs:78-136)
+        float de = FLT_MAX;
+        if (lane < count) de = sm.P[0][lane] * axis[0] + sm.P[1][lane] * axis[1] + sm.P[2][lane] * axis[2];
+        if (lane < 16) sm.D[lane] = de;
+        tm.sync();
+        if (lane < 16) {
+            int rank = 0;
+#pragma unroll
+            for (int f = 0; f < 16; ++f) {
+                const float df = sm.D[f];
+                rank += (dps_less(df, de) || (f < lane && dps_equiv(df, de))) ? 1 : 0;
+            }
+            reinterpret_cast<uint8_t *>(sm.hist[it])[rank] = (uint8_t)(lane < count ? lane : 0);
+        }
+        tm.sync();
+        const int my_ord = (lane < 16) ? hist_get(sm, it, lane) : 0;
+        bool repeated = false;
+#pragma unroll 1
+        for (int t = 0; t < it; ++t) repeated |= tm.all(lane >= 16 || hist_get(sm, t, lane) == my_ord);
+        if (repeated) break;
+        if (lane < count) {
+            const float w = sm.P[3][my_ord];
+            sm.PW[lane] = make_float4(sm.P[0][my_ord] * w, sm.P[1][my_ord] * w, sm.P[2][my_ord] * w, 1.0f * w);
+        }
+        tm.sync();
+        // partial sums S(a,b) = pw[a] + ... + pw[b-1], accumulated from zero in
+        // loop order exactly like part0/part1/part2 of the reference
+        if (lane == 0) sm.S[tri_idx(count, count)] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (lane < count) {
+            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+            sm.S[tri_idx(lane, lane)] = acc;
+            const int o = tri_off(lane) - lane;
+            for (int b = lane; b < count; ++b) {
+                const float4 q = sm.PW[b];
+                acc.x += q.x; acc.y += q.y; acc.z += q.z; acc.w += q.w;
+                sm.S[o + b + 1] = acc;
+            }
+        }
+        tm.sync();
+        xs = sm.S[count];  // S(0, count) == xsum_wsum
+
+        // the sweep: lane-strided over the candidate list
+        float lbest = __int_as_float(0x7f800000);
+        uint32_t lent = 0xFFFFFFFFu;
+        float dummy_a[3], dummy_b[3];
+        for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
+            const uint32_t e = tbl[t];
+            const float4 p0 = sm.S[e & 0xFu];
+            const float4 p1 = sm.S[(e >> 4) & 0xFFu];
+            float err;
+            if (NC == 4) {
+                const float4 p2 = sm.S[(e >> 12) & 0xFFu];
+                err = eval4<false>(p0, p1, p2, xs, cw, dummy_a, dummy_b);
+            } else {
+                err = eval3<false>(p0, p1, xs, cw, dummy_a, dummy_b);
+            }
+            if (err < run && (err < lbest || (err == lbest && e < lent))) { lbest = err; lent = e; }
+        }
+#pragma unroll
+        for (int off = TEAM / 2; off > 0; off >>= 1) {
+            const float oe = tm.shfl_xor(lbest, off);
+            const uint32_t on = tm.shfl_xor(lent, off);
+            if (oe < lbest || (oe == lbest && on < lent)) { lbest = oe; lent = on; }
+        }
+        if (lent != 0xFFFFFFFFu) {
+            run = lbest;
+            bentry = lent;
+            bit = it;
+            const float4 p0 = sm.S[lent & 0xFu];
+            const float4 p1 = sm.S[(lent >> 4) & 0xFFu];
+            if (NC == 4) {
+                const float4 p2 = sm.S[(lent >> 12) & 0xFFu];
+                eval4<true>(p0, p1, p2, xs, cw, ba, bb);
+            } else {
+                eval3<true>(p0, p1, xs, cw, ba, bb);
+            }
+        }
+        if (bit != it) break;
+        axis[0] = bb[0] - ba[0]; axis[1] = bb[1] - ba[1]; axis[2] = bb[2] - ba[2];
+    }
+
+    if (run < best_err) {
+        int i, j, k;
+        decode_entry(bentry, i, j, k);
+        uint32_t ind = 3;
+        if (valid) {
+            int maxpos = -1;
+            for (int m = 0; m < count; ++m) maxpos = (hist_get(sm, bit, m) == my_point) ? m : maxpos;
+            if (NC == 4) ind = maxpos >= k ? 1u : maxpos >= j ? 3u : maxpos >= i ? 2u : 0u;
+            else ind = maxpos >= j ? 1u : maxpos >= i ? 2u : 0u;
+        }
+        const uint32_t word = __reduce_or_sync(tm.mask, lane < 16 ? (ind << (2 * lane)) : 0u);
+        const uint32_t a565 = pack_565(ba[0], ba[1], ba[2]), b565 = pack_565(bb[0], bb[1], bb[2]);
+        best = (NC == 4) ? write4(a565, b565, word) : write3(a565, b565, word);
+        best_err = run;
+    }
+}
+
+template <int FMT, int TEAM, int NITER>
+__device__ __forceinline__ uint2 colour_cluster_team(const Team<TEAM> &tm, TeamSmem &sm, const uint32_t *tbl4,
+                                                     const uint32_t *tbl3, uint32_t px, bool inb,
+                                                     const DevParams &prm) {
+    const int lane = tm.lane;
+    const uint32_t a = px >> 24;
+    const bool tr = (FMT == BC1) && inb && a < 128u;
+    const bool valid = inb && !tr;
+    const bool transparent = tm.ballot(tr) != 0u;
+    const uint32_t key = valid ? (px & 0xFFFFFFu) : (0x01000000u | (uint32_t)lane);
+    const unsigned eq = tm.match(key);
+    const int first = __ffs(eq) - 1;
+    const bool is_new = valid && first == lane;
+    const unsigned newbits = tm.ballot(is_new);
+    const int count = __popc(newbits);
+    const int my_point = valid ? __popc(newbits & ((1u << first) - 1u)) : -1;
+
+    // weights: count of equal pixels, or alpha weights summed in pixel order
+    float wsum;
+    if (!prm.alpha_weighted) {
+        wsum = (float)__popc(eq);
+    } else {
+        const float wa = (float)(a + 1u) * (1.0f / 256.0f);
+        const int fv = valid ? first : -1;
+        wsum = 0.0f;
+#pragma unroll
+        for (int q = 0; q < 16; ++q) {
+            const float wq = tm.shfl(wa, q);
+            const int fq = tm.shfl(fv, q);
+            wsum = wsum + ((fq == lane) ? wq : 0.0f);
+        }
+    }
+    if (is_new) {
+        sm.P[0][my_point] = unorm8(px & 0xFFu);
+        sm.P[1][my_point] = unorm8((px >> 8) & 0xFFu);
+        sm.P[2][my_point] = unorm8((px >> 16) & 0xFFu);
+        sm.P[3][my_point] = sqrt_rn(wsum);
+    }
+    tm.sync();
+
+    const uint32_t valid16 = tm.ballot(valid);
+    if (count == 1) {
+        int col[3];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) col[c] = f32_to_i32_clamped(sm.P[c][0] * 255.0f, 255);
+        return single_fit<FMT>(col, valid16, transparent);
+    }
+    if (count == 0) {
+        // RangeFit on an empty set (range.rs:67-98): start = end = 0, error 0.
+        // BC1: compress3 writes (0, 0) with every pixel excluded -> index 3;
+        // compress4 never wins against error 0.  BC2/3: write4 with a == b.
+        return (FMT == BC1) ? make_uint2(0u, 0xFFFFFFFFu) : make_uint2(0u, 0u);
+    }
+
+    // Sym3x3::weighted_covariance (math.rs:44-73), terms split over lanes
+    float total = 0.0f;
+    for (int k = 0; k < count; ++k) total = total + sm.P[3][k];
+    const int ch = lane < 3 ? lane : 0;
+    float cs = 0.0f;
+    for (int k = 0; k < count; ++k) cs = cs + sm.P[ch][k] * sm.P[3][k];
+    float cen[3] = {tm.shfl(cs, 0), tm.shfl(cs, 1), tm.shfl(cs, 2)};
+    if (total > FLT_EPSILON) { cen[0] = div_rn(cen[0], total); cen[1] = div_rn(cen[1], total); cen[2] = div_rn(cen[2], total); }
+    const int term = lane < 6 ? lane : 0;
+    const int c1 = term < 3 ? 0 : (term < 5 ? 1 : 2);
+    const int c2 = term < 3 ? term : (term < 5 ? term - 2 : 2);
+    const float m1 = c1 == 0 ? cen[0] : (c1 == 1 ? cen[1] : cen[2]);
+    const float m2 = c2 == 0 ? cen[0] : (c2 == 1 ? cen[1] : cen[2]);
+    float cv = 0.0f;
+    for (int k = 0; k < count; ++k) {
+        const float a1 = sm.P[c1][k] - m1;
+        const float a2 = sm.P[c2][k] - m2;
+        const float b2 = a2 * sm.P[3][k];
+        cv += a1 * b2;
+    }
+    float cov[6];
+#pragma unroll
+    for (int t = 0; t < 6; ++t) cov[t] = tm.shfl(cv, t);
+    float principal[3];
+    principle_component(cov, principal);
+
+    const float cw[3] = {prm.w[0], prm.w[1], prm.w[2]};
+    float best_err = FLT_MAX;
+    uint2 best = make_uint2(0u, 0u);
+    if (FMT == BC1) {
+        cluster_pass<3, TEAM, NITER>(tm, sm, tbl3, count, principal, cw, valid, my_point, best_err, best);
+        if (!transparent)
+            cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, valid, my_point, best_err, best);
+    } else {
+        cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, valid, my_point, best_err, best);
+    }
+    return best;
+}
+
+template <int TEAM>
+__device__ __forceinline__ uint2 team_bc3_alpha(const Team<TEAM> &tm, uint32_t v, bool inb) {
+    const int lane = tm.lane;
+    int min7 = (int)__reduce_min_sync(tm.mask, inb ? v : 255u);
+    int max7 = (int)__reduce_max_sync(tm.mask, inb ? v : 0u);
+    int min5 = (int)__reduce_min_sync(tm.mask, (inb && v != 0u) ? v : 255u);
+    int max5 = (int)__reduce_max_sync(tm.mask, (inb && v != 255u) ? v : 0u);
+    if (min5 > max5) min5 = max5;
+    if (min7 > max7) min7 = max7;
+    fix_range(min5, max5, 5);
+    fix_range(min7, max7, 7);
+    int c5[8], c7[8];
+    c5[0] = min5; c5[1] = max5;
+#pragma unroll
+    for (int i = 1; i < 5; ++i) c5[1 + i] = ((5 - i) * min5 + i * max5) / 5;
+    c5[6] = 0; c5[7] = 255;
+    c7[0] = min5; c7[1] = max5;
+#pragma unroll
+    for (int i = 1; i < 7; ++i) c7[1 + i] = ((7 - i) * min7 + i * max7) / 7;
+    int i5 = 0, i7 = 0, d5 = abs((int)v - c5[0]), d7 = abs((int)v - c7[0]);
+#pragma unroll
+    for (int j = 1; j < 8; ++j) {
+        const int e5 = abs((int)v - c5[j]), e7 = abs((int)v - c7[j]);
+        if (e5 < d5) { d5 = e5; i5 = j; }
+        if (e7 < d7) { d7 = e7; i7 = j; }
+    }
+    if (!inb) { i5 = 0; i7 = 0; d5 = 0; d7 = 0; }
+    const uint32_t err5 = __reduce_add_sync(tm.mask, (uint32_t)(d5 * d5));
+    const uint32_t err7 = __reduce_add_sync(tm.mask, (uint32_t)(d7 * d7));
+    uint32_t a0, a1, idx;
+    if (err5 <= err7) {
+        a0 = (uint32_t)min5; a1 = (uint32_t)max5; idx = (uint32_t)i5;
+        if (min5 > max5) {  // never true after fix_range (alpha.rs:146-165)
+            a0 = (uint32_t)max5; a1 = (uint32_t)min5;
+            idx = idx == 0 ? 1u : idx == 1 ? 0u : (idx <= 5 ? 7u - idx : idx);
+        }
+    } else {
+        a0 = (uint32_t)min7; a1 = (uint32_t)max7; idx = (uint32_t)i7;
+        if (min7 < max7) { a0 = (uint32_t)max7; a1 = (uint32_t)min7; idx = (9u - idx) & 7u; }
+    }
+    const uint32_t lo = __reduce_or_sync(tm.mask, (lane < 8) ? (idx << (3 * lane)) : 0u);
+    const uint32_t hi = __reduce_or_sync(tm.mask, (lane >= 8 && lane < 16) ? (idx << (3 * (lane - 8))) : 0u);
+    return make_uint2(a0 | (a1 << 8) | ((lo & 0xFFFFu) << 16), (lo >> 16) | (hi << 8));
+}
+
+
+// ===========================================================================
+// block-level entry points
+
+// Thread-per-block: encode and store block b (RangeFit / SingleColourFit path).
+template <int FMT>
+__device__ __forceinline__ void range_block(const SrcDesc &src, size_t b, const DevParams &prm, uint8_t *out,
+                                            const float *s_unorm, const float *s_sqrt) {
+    uint32_t px[16];
+    const uint32_t mask = load_block_rgba(src, b, px);
+    const uint2 col = colour_range_thread<FMT>(px, mask, prm, s_unorm, s_sqrt);
+    if (FMT == BC1) {
+        reinterpret_cast<uint2 *>(out)[b] = col;
+    } else {
+        uint2 al = (FMT == BC2) ? encode_bc2_alpha(px, mask) : make_uint2(0u, 0u);
+        if (FMT == BC3) {
+            uint32_t v[4];
+            channel_words(px, 3, v);
+            al = encode_bc3_alpha(v, mask);
+        }
+        reinterpret_cast<uint4 *>(out)[b] = make_uint4(al.x, al.y, col.x, col.y);
+    }
+}
+
+// Team-per-block: encode and store block b (ClusterFit path).
+template <int FMT, int TEAM, int NITER>
+__device__ __forceinline__ void cluster_block(const Team<TEAM> &tm, TeamSmem &sm, const uint32_t *tbl4,
+                                              const uint32_t *tbl3, const SrcDesc &src, size_t b,
+                                              const DevParams &prm, uint8_t *out) {
+    const int p = tm.lane;
+    uint32_t px = 0;
+    bool inb = false;
+    if (p < 16) {
+        if (src.mode == 1) {
+            px = __ldg(reinterpret_cast<const uint32_t *>(src.base + 64 * b) + p);
+            inb = src.masks ? ((__ldg(src.masks + b) >> p) & 1u) : true;
+        } else {
+            const uint32_t bx = (uint32_t)(b % src.blocks_wide), by = (uint32_t)(b / src.blocks_wide);
+            const uint32_t x = 4 * bx + (p & 3), y = 4 * by + (p >> 2);
+            inb = x < src.width && y < src.height;
+            if (inb) px = ld_u32_any(src.base + (size_t)y * src.pitch + 4 * (size_t)x);
+        }
+    }
+    uint2 al = make_uint2(0u, 0u);
+    if (FMT == BC2) {
+        const uint32_t q = inb ? bc2_quant(px >> 24) : 0u;
+        al.x = __reduce_or_sync(tm.mask, p < 8 ? q << (4 * p) : 0u);
+        al.y = __reduce_or_sync(tm.mask, (p >= 8 && p < 16) ? q << (4 * (p - 8)) : 0u);
+    } else if (FMT == BC3) {
+        al = team_bc3_alpha<TEAM>(tm, px >> 24, inb);
+    }
+    const uint2 col = colour_cluster_team<FMT, TEAM, NITER>(tm, sm, tbl4, tbl3, px, inb, prm);
+    if (p == 0) {
+        if (FMT == BC1) reinterpret_cast<uint2 *>(out)[b] = col;
+        else reinterpret_cast<uint4 *>(out)[b] = make_uint4(al.x, al.y, col.x, col.y);
+    }
+    tm.sync();
+}
+
+constexpr int kCandTbl = kCand4 + 1 + kCand3 + 1;
+constexpr size_t kCandTblBytes = (size_t)((kCandTbl * 4 + 15) & ~15);
+
+// Copy the candidate lists of this TU into shared memory (whole CTA).
+__device__ __forceinline__ void load_cand_tables(uint32_t *tbl) {
+    for (int i = threadIdx.x; i < kCandTbl; i += blockDim.x) tbl[i] = g_cand[i];
+}
+
+// ===========================================================================
+// host side: candidate lists + upload of this TU's tables
+
+// Build the candidate lists and single-colour tables and copy them to the
+// current device.
+static inline cudaError_t upload_tables_this_tu(const uint32_t lut[4][256][2]) {
+    // compress4: (i, j, k), 0 <= i < 16, i <= j <= 16, max(j,1) <= k <= 16
+    struct C { int m, rank; uint32_t e; };
+    C c4[kCand4], c3[kCand3];
+    int n4 = 0, n3 = 0;
+    for (int i = 0; i < 16; ++i)
+        for (int j = i; j <= 16; ++j)
+            for (int k = (j == 0 ? 1 : j); k <= 16; ++k) {
+                const int m = (i + 1 > j ? i + 1 : j) > k ? (i + 1 > j ? i + 1 : j) : k;
+                c4[n4].m = m;
+                c4[n4].rank = n4;
+                c4[n4].e = (uint32_t)i | ((uint32_t)tri_idx(i, j) << 4) | ((uint32_t)tri_idx(j, k) << 12) |
+                           ((uint32_t)n4 << 20);
+                ++n4;
+            }
+    for (int i = 0; i < 16; ++i)
+        for (int j = (i == 0 ? 1 : i); j <= 16; ++j) {
+            const int m = i + 1 > j ? i + 1 : j;
+            c3[n3].m = m;
+            c3[n3].rank = n3;
+            c3[n3].e = (uint32_t)i | ((uint32_t)tri_idx(i, j) << 4) | ((uint32_t)n3 << 20);
+            ++n3;
+        }
+    if (n4 != kCand4 || n3 != kCand3) return cudaErrorInvalidValue;
+    auto sort_by_m = [](C *v, int n) {
+        for (int a = 1; a < n; ++a) {  // stable insertion sort on m
+            C t = v[a];
+            int b = a;
+            while (b > 0 && v[b - 1].m > t.m) { v[b] = v[b - 1]; --b; }
+            v[b] = t;
+        }
+    };
+    sort_by_m(c4, n4);
+    sort_by_m(c3, n3);
+    uint32_t tbl[kCand4 + 1 + kCand3 + 1] = {};
+    uint32_t nc4[17] = {}, nc3[17] = {};
+    for (int t = 0; t < kCand4; ++t) tbl[t] = c4[t].e;
+    for (int t = 0; t < kCand3; ++t) tbl[kCand4 + 1 + t] = c3[t].e;
+    for (int n = 0; n <= 16; ++n) {
+        for (int t = 0; t < kCand4; ++t) nc4[n] += c4[t].m <= n ? 1u : 0u;
+        for (int t = 0; t < kCand3; ++t) nc3[n] += c3[t].m <= n ? 1u : 0u;
+    }
+    cudaError_t e;
+    if ((e = cudaMemcpyToSymbol(g_cand, tbl, sizeof(tbl))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(c_ncand4, nc4, sizeof(nc4))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(c_ncand3, nc3, sizeof(nc3))) != cudaSuccess) return e;
+    return cudaMemcpyToSymbol(c_lut, lut, sizeof(uint32_t) * 4 * 256 * 2);
+}
+
+
+}  // namespace tx

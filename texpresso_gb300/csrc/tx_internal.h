@@ -27,6 +27,9 @@ cudaError_t launch_colour(int fmt, int algorithm, const SrcDesc &src, const DevP
                           size_t nblocks, cudaStream_t st, const LaunchCfg &cfg);
 size_t cluster_smem_bytes(int team, int threads);
 
+// tx_batch.cu
+cudaError_t upload_batch_tables(const uint32_t lut[4][256][2]);
+
 // tx_alpha.cu
 cudaError_t launch_alpha(int fmt, const SrcDesc &src, uint8_t *out, size_t nblocks, cudaStream_t st,
                          const LaunchCfg &cfg);
@@ -36,3 +39,7 @@ cudaError_t launch_decode(int fmt, const uint8_t *data, size_t blocks_wide, size
                           size_t height, uint8_t *out, size_t out_pitch, size_t out_len, cudaStream_t st);
 
 }  // namespace tx
+
+// tx_api.cu: shared device bookkeeping for every entry point
+int tx_internal_ensure_device();                // tables uploaded on the current device
+void tx_internal_set_last_cuda_error(int err);  // for tx_last_cuda_error()

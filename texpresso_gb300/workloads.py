@@ -144,3 +144,59 @@ def random_blocks(n, seed=0):
             v[:, 3] = rng.choice([0, 127, 128, 255], size=16)
             out[b] = v
     return out.reshape(n, 64)
+
+
+# ---------------------------------------------------------------------------
+# batched configuration: many textures of uneven sizes with mip chains
+
+def batch_specs(n=1000, seed=0, min_side=4, max_side=4096, formats=(0, 2, 4), algorithms=(0, 1, 2)):
+    """Texture specs: width and height log-uniform in [min_side, max_side]
+    (non-multiples of 4 allowed), format and algorithm drawn uniformly."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log(min_side), np.log(max_side + 1)
+    ws = np.floor(np.exp(rng.uniform(lo, hi, n))).astype(int).clip(min_side, max_side)
+    hs = np.floor(np.exp(rng.uniform(lo, hi, n))).astype(int).clip(min_side, max_side)
+    fm = rng.choice(formats, n)
+    al = rng.choice(algorithms, n)
+    return [{"width": int(w), "height": int(h), "format": int(f), "algorithm": int(a), "seed": int(seed * 100003 + i)}
+            for i, (w, h, f, a) in enumerate(zip(ws, hs, fm, al))]
+
+
+def ramp_texture_torch(width, height, seed, device, flat_frac=0.10, sigma=6.0, alpha="ramp"):
+    """ramp_texture's distribution generated with torch on `device` (fast for
+    large batches; the values differ from the numpy generator's)."""
+    import torch
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    bw, bh = (width + 3) // 4, (height + 3) // 4
+    nb = bw * bh
+    u = lambda *s: torch.rand(*s, generator=g, device=device)
+    c0 = u(nb, 1, 3) * 255
+    c1 = u(nb, 1, 3) * 255
+    col = c0 + u(nb, 16, 1) * (c1 - c0) + torch.randn(nb, 16, 3, generator=g, device=device) * sigma
+    flat = u(nb) < flat_frac
+    col = torch.where(flat[:, None, None], c0.expand(nb, 16, 3), col)
+    col = col.round().clamp(0, 255).to(torch.uint8)
+    if alpha == "ramp":
+        a0, a1 = u(nb, 1) * 255, u(nb, 1) * 255
+        pos = ((torch.arange(16, device=device) % 4 + torch.arange(16, device=device) // 4) / 6.0)[None, :]
+        av = a0 + (a1 - a0) * pos + torch.randint(-12, 13, (nb, 16), generator=g, device=device)
+        a = av.round().clamp(0, 255).to(torch.uint8)[..., None]
+    else:
+        a = torch.full((nb, 16, 1), 255, dtype=torch.uint8, device=device)
+    blocks = torch.cat([col, a], dim=2).reshape(bh, bw, 4, 4, 4)
+    img = blocks.permute(0, 2, 1, 3, 4).reshape(bh * 4, bw * 4, 4)
+    return img[:height, :width].contiguous()
+
+
+def mip_reference(img):
+    """Next mip level of an (h, w, c) u8 image with the library's box filter:
+    (a+b+c+d+2)>>2 over the 2x2 source footprint, coordinates clamped."""
+    h, w, c = img.shape
+    dw, dh = max(1, w // 2), max(1, h // 2)
+    xs0 = np.minimum(2 * np.arange(dw), w - 1)
+    xs1 = np.minimum(2 * np.arange(dw) + 1, w - 1)
+    ys0 = np.minimum(2 * np.arange(dh), h - 1)
+    ys1 = np.minimum(2 * np.arange(dh) + 1, h - 1)
+    s = (img[ys0][:, xs0].astype(np.uint32) + img[ys0][:, xs1] + img[ys1][:, xs0] + img[ys1][:, xs1])
+    return ((s + 2) >> 2).astype(np.uint8)
