@@ -186,6 +186,23 @@ TX_API int tx_batch_autotune(tx_batch *batch, void *stream, int repeats, tx_batc
 
 TX_API void tx_batch_destroy(tx_batch *batch);
 
+/* Allocation-free batch launch.  No counterpart in the reference.  For
+ * callers that must not have a library allocate device memory -- engines that
+ * reserve the whole memory budget up front and hand it out through their own
+ * allocator, or per-frame loops that cannot take the implicit synchronisation
+ * of an allocation or free.  Compresses up to 256 texture levels exactly as
+ * tx_batch_create + tx_batch_launch would, but keeps the work queue in a
+ * fixed 1 MiB array of device memory that the library declares statically
+ * (every GPU that loads the library holds it until the process exits), so the
+ * call itself allocates nothing.  The caller passes inputs and outputs as in
+ * tx_batch_item.  More than 256 items returns TX_ERR_INVALID_ARGUMENT.
+ * Stream-ordered.  The first call on each device does a one-time set-up with
+ * that device current (it looks up the array's device address); make that
+ * first call before any stream capture.  All calls share the array, so calls
+ * whose work overlaps on the GPU (other streams or threads) race: order them
+ * on one stream. */
+TX_API int tx_batch_launch_noalloc(const tx_batch_item *items, size_t nitems, void *stream);
+
 /* Mip producer (the reference builds no mips, cli/src/main.rs:153): one level
  * step, next = max(1, size / 2) per axis, each output channel the 2x2 box
  * average (a+b+c+d+2)>>2 of the source with coordinates clamped at odd edges. */

@@ -26,6 +26,7 @@
 #include <algorithm>
 #include <chrono>
 #include <cstring>
+#include <mutex>
 #include <new>
 #include <vector>
 
@@ -540,3 +541,212 @@ void tx_batch_destroy(tx_batch *b) {
 }
 
 }  // extern "C"
+
+// ===========================================================================
+// Allocation-free variant of the batch launch.
+//
+// Some callers cannot let a library call cudaMalloc: engines that reserve the
+// whole device memory budget up front and hand out memory only through their
+// own allocator, and per-frame loops that cannot afford the implicit device
+// synchronisation an allocation or free may cause.  For them
+// tx_batch_launch_noalloc compresses up to kNoallocMaxItems texture levels
+// with the persistent batch kernels above, keeping the work queue (two
+// counters, the item table, the units) in one file-scope device array of
+// fixed size instead of memory from cudaMalloc.  Every GPU that loads this
+// library holds the array until the process exits.  All calls share it and
+// it keeps the last call's contents, so the set-up kernel clears the counters
+// at the start of every call, and calls whose work overlaps on the GPU (two
+// streams, or two host threads) race on it.
+
+namespace tx {
+
+constexpr size_t kNoallocScratchBytes = (size_t)1 << 20;  // 1 MiB per device
+constexpr uint32_t kNoallocMaxItems = 256;                // texture levels per call
+constexpr size_t kNoallocItemsOff = 256;                  // after the two counters
+constexpr size_t kNoallocUnitsOff =
+    (kNoallocItemsOff + kNoallocMaxItems * sizeof(BatchItem) + 255) & ~(size_t)255;
+constexpr uint32_t kNoallocMaxUnits = (uint32_t)((kNoallocScratchBytes - kNoallocUnitsOff) / sizeof(uint2));
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoallocScratchBytes];
+
+struct NoallocSetup {
+    BatchItem items[kNoallocMaxItems];
+    uint32_t nitems;
+    uint32_t lane_span;  // blocks per lane unit (a multiple of 32)
+    uint32_t team_span;  // blocks per team unit
+};
+
+// One CTA: copy the item table into the scratch array, clear the counters and
+// write both unit queues (lane units first, then team units in item order).
+__global__ void __launch_bounds__(kNoallocMaxItems) k_noalloc_setup(const __grid_constant__ NoallocSetup p) {
+    uint32_t *counters = reinterpret_cast<uint32_t *>(g_noalloc_scratch);
+    BatchItem *items = reinterpret_cast<BatchItem *>(g_noalloc_scratch + kNoallocItemsOff);
+    uint2 *units = reinterpret_cast<uint2 *>(g_noalloc_scratch + kNoallocUnitsOff);
+    __shared__ uint32_t sl[kNoallocMaxItems], stm[kNoallocMaxItems];
+    const uint32_t t = threadIdx.x;
+    if (t < 2) counters[t] = 0;
+    uint32_t nl = 0, nt = 0;
+    if (t < p.nitems) {
+        const BatchItem &it = p.items[t];
+        items[t] = it;
+        if (it.kind == KIND_ALPHA || it.kind == KIND_RANGE) nl = (it.nblocks + p.lane_span - 1) / p.lane_span;
+        else nt = (it.nblocks + p.team_span - 1) / p.team_span;
+    }
+    sl[t] = nl;
+    stm[t] = nt;
+    __syncthreads();
+    for (uint32_t off = 1; off < kNoallocMaxItems; off <<= 1) {
+        const uint32_t a = t >= off ? sl[t - off] : 0u, b = t >= off ? stm[t - off] : 0u;
+        __syncthreads();
+        sl[t] += a;
+        stm[t] += b;
+        __syncthreads();
+    }
+    const uint32_t lane_base = sl[t] - nl;
+    const uint32_t team_base = sl[kNoallocMaxItems - 1] + stm[t] - nt;
+    for (uint32_t k = 0; k < nl; ++k) units[lane_base + k] = make_uint2(t, k * p.lane_span);
+    for (uint32_t k = 0; k < nt; ++k) units[team_base + k] = make_uint2(t, k * p.team_span);
+}
+
+}  // namespace tx
+
+namespace {
+
+struct NoallocDevice {
+    bool ready = false;
+    unsigned char *scratch = nullptr;  // device address of g_noalloc_scratch
+    int sm_count = 0;
+};
+NoallocDevice g_noalloc_dev[64];
+std::mutex g_noalloc_mu;
+
+// Per-device set-up, done by the first call on each device (with that device
+// current): the device address of the scratch array, the SM count and the
+// team kernel's shared-memory limit.
+int noalloc_setup_device(int dev, NoallocDevice **out) {
+    std::lock_guard<std::mutex> lk(g_noalloc_mu);
+    NoallocDevice &d = g_noalloc_dev[dev];
+    if (!d.ready) {
+        void *ptr = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&ptr, tx::g_noalloc_scratch);
+        if (e != cudaSuccess) return fail_batch(e);
+        if ((e = cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+            return fail_batch(e);
+        if ((e = cudaFuncSetAttribute(tx::k_batch_teams<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)tx::cluster_smem_bytes(32, 1024))) != cudaSuccess)
+            return fail_batch(e);
+        d.scratch = static_cast<unsigned char *>(ptr);
+        d.ready = true;
+    }
+    *out = &d;
+    return TX_OK;
+}
+
+}  // namespace
+
+extern "C" int tx_batch_launch_noalloc(const tx_batch_item *items, size_t nitems, void *stream) {
+    if (nitems == 0) return TX_OK;
+    if (!items || nitems > tx::kNoallocMaxItems) return TX_ERR_INVALID_ARGUMENT;
+    static_assert(sizeof(tx::NoallocSetup) <= 32000, "kernel parameter block too large");
+    tx::NoallocSetup setup;
+    std::memset(&setup, 0, sizeof(setup));
+    // order: lane items and iterative ClusterFit items first, so the team
+    // queue starts with its most expensive units
+    uint32_t n = 0;
+    uint64_t lane_blocks = 0, team_blocks = 0;
+    for (int pass = 0; pass < 2; ++pass) {
+        for (size_t i = 0; i < nitems; ++i) {
+            const tx_batch_item &it = items[i];
+            const size_t bs = tx_block_size(it.format);
+            const bool ch_ok = it.channels == 4 || (it.channels == 1 && it.format == TX_FORMAT_BC4) ||
+                               (it.channels == 2 && it.format == TX_FORMAT_BC5);
+            const int alg = it.params.algorithm;
+            if (bs == 0) return TX_ERR_INVALID_FORMAT;
+            if (!ch_ok || alg < TX_RANGE_FIT || alg > TX_ITERATIVE_CLUSTER_FIT || it.width == 0 ||
+                it.src_pitch < (size_t)it.width * it.channels || (it.height && !it.src) || !it.dst)
+                return TX_ERR_INVALID_ARGUMENT;
+            if ((reinterpret_cast<uintptr_t>(it.dst) % bs) != 0) return TX_ERR_MISALIGNED;
+            const size_t nb = tx_num_blocks(it.width) * tx_num_blocks(it.height);
+            if (nb > 0xFFFFFFF0u) return TX_ERR_INVALID_ARGUMENT;
+            const bool lane = it.format == TX_FORMAT_BC4 || it.format == TX_FORMAT_BC5 || alg == TX_RANGE_FIT;
+            const bool first = lane || alg == TX_ITERATIVE_CLUSTER_FIT;
+            if (first != (pass == 0)) continue;
+            tx::BatchItem &d = setup.items[n++];
+            d.src.base = static_cast<const uint8_t *>(it.src);
+            d.src.masks = nullptr;
+            d.src.pitch = it.src_pitch;
+            d.src.width = it.width;
+            d.src.height = it.height;
+            d.src.blocks_wide = (uint32_t)tx_num_blocks(it.width);
+            d.src.channels = it.channels;
+            const size_t va = it.channels == 4 ? 16 : (size_t)it.channels * 4;
+            d.src.vec16 = ((reinterpret_cast<uintptr_t>(it.src) % va) == 0 && (it.src_pitch % va) == 0) ? 1 : 0;
+            d.src.mode = 0;
+            for (int c = 0; c < 3; ++c) d.prm.w[c] = it.params.weights[c];
+            d.prm.alpha_weighted = it.params.weigh_colour_by_alpha ? 1 : 0;
+            d.dst = static_cast<uint8_t *>(it.dst);
+            d.nblocks = (uint32_t)nb;
+            d.format = it.format;
+            d.channels = it.channels;
+            d.kind = lane ? (alg == TX_RANGE_FIT && it.format <= TX_FORMAT_BC3 ? tx::KIND_RANGE : tx::KIND_ALPHA)
+                          : (alg == TX_ITERATIVE_CLUSTER_FIT ? tx::KIND_CLUSTER_ITER : tx::KIND_CLUSTER);
+            (lane ? lane_blocks : team_blocks) += nb;
+        }
+    }
+    setup.nitems = n;
+    // unit sizes: the defaults, doubled until both queues fit the scratch array
+    uint32_t lane_span = 64, team_span = 1;
+    auto count_units = [&](uint64_t *nl, uint64_t *nt) {
+        *nl = *nt = 0;
+        for (uint32_t i = 0; i < n; ++i) {
+            const tx::BatchItem &d = setup.items[i];
+            if (d.kind == tx::KIND_ALPHA || d.kind == tx::KIND_RANGE) *nl += (d.nblocks + lane_span - 1) / lane_span;
+            else *nt += (d.nblocks + team_span - 1) / team_span;
+        }
+    };
+    uint64_t n_lane = 0, n_team = 0;
+    count_units(&n_lane, &n_team);
+    while (n_lane + n_team > tx::kNoallocMaxUnits) {
+        if (n_team >= n_lane) team_span *= 2;
+        else lane_span *= 2;
+        count_units(&n_lane, &n_team);
+    }
+    setup.lane_span = lane_span;
+    setup.team_span = team_span;
+    (void)lane_blocks;
+    (void)team_blocks;
+
+    int rc = tx_internal_ensure_device();
+    if (rc != TX_OK) return rc;
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return fail_batch(e);
+    if (dev < 0 || dev >= 64) return TX_ERR_NO_DEVICE;
+    NoallocDevice *nd = nullptr;
+    if ((rc = noalloc_setup_device(dev, &nd)) != TX_OK) return rc;
+
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    const tx::BatchItem *d_items = reinterpret_cast<const tx::BatchItem *>(nd->scratch + tx::kNoallocItemsOff);
+    const uint2 *d_units = reinterpret_cast<const uint2 *>(nd->scratch + tx::kNoallocUnitsOff);
+    uint32_t *d_counters = reinterpret_cast<uint32_t *>(nd->scratch);
+    tx::k_noalloc_setup<<<1, tx::kNoallocMaxItems, 0, st>>>(setup);
+    tx::note_launch();
+    if ((e = cudaGetLastError()) != cudaSuccess) return fail_batch(e);
+    if (n_lane) {
+        tx::BatchQueue q{d_items, d_units, (uint32_t)n_lane, d_counters, lane_span / 32};
+        uint32_t grid = (uint32_t)(nd->sm_count * 3);
+        grid = std::min<uint32_t>(grid, (uint32_t)((n_lane + 3) / 4));
+        tx::k_batch_lanes<<<grid, 128, 0, st>>>(q);
+        tx::note_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail_batch(e);
+    }
+    if (n_team) {
+        tx::BatchQueue q{d_items, d_units + n_lane, (uint32_t)n_team, d_counters + 1, team_span};
+        uint32_t grid = (uint32_t)(nd->sm_count * 3);
+        grid = std::min<uint32_t>(grid, (uint32_t)((n_team + 7) / 8));
+        tx::k_batch_teams<32><<<grid, 256, tx::cluster_smem_bytes(32, 256), st>>>(q);
+        tx::note_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return fail_batch(e);
+    }
+    return TX_OK;
+}
