@@ -66,6 +66,7 @@ def parse():
     ap.add_argument("--size", type=int, default=2048)
     ap.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU-baseline sample length")
     ap.add_argument("--batched-only", action="store_true", help="run only the config-3 batched comparison")
+    ap.add_argument("--serving-only", action="store_true", help="run only the config-4 serving comparison")
     ap.add_argument("--case", default=None,
                     help="time one extra workload only (device timing, no CPU leg); for profiling: " +
                          ", ".join(CASES))
@@ -418,6 +419,7 @@ def run_ours(args):
         if not args.no_extra:
             line["extra"] = extras(torch, tx, oracle, args, hbm_peak, fp32_peak_tops)
             line["batched"] = batched(torch, tx, args)
+            line["serving"] = serving(torch, tx, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world_size > 1:
@@ -578,6 +580,119 @@ def batched(torch, tx, args, n_textures=1000):
     return rec
 
 
+def serving(torch, tx, args, n_req=48, rates=(100, 300, 1000, 5000)):
+    """Config 4: Poisson arrivals of requests (RGBA8, side log-uniform 64..8192,
+    full mip chain, BC1/BC3/BC5 with IterativeClusterFit), served with a 40 GB
+    admission budget and continuous batching, against the plain path that
+    handles one request at a time (copy in, mips, one tx_compress_device per
+    level, copy out)."""
+    from texpresso_gb300 import workloads
+    rng = np.random.default_rng(7)
+    sides = np.floor(np.exp(rng.uniform(np.log(64), np.log(8193), n_req))).astype(int).clip(64, 8192)
+    fmts = [(0, 2, 4)[k % 3] for k in range(n_req)]
+    params = tx.Params(algorithm=tx.Algorithm.IterativeClusterFit)
+    imgs = [workloads.ramp_texture_torch(int(sd), int(sd), seed=900 + k, device="cuda").cpu().pin_memory()
+            for k, sd in enumerate(sides)]
+    sizes = [tx.chain_compressed_size(f, int(sd), int(sd)) for f, sd in zip(fmts, sides)]
+    out_srv = [torch.empty(n, dtype=torch.uint8).pin_memory() for n in sizes]
+    out_plain = [torch.empty(n, dtype=torch.uint8).pin_memory() for n in sizes]
+    blocks = []
+    for sd in sides:
+        w = h = int(sd)
+        nb = 0
+        while True:
+            nb += tx.num_blocks(w) * tx.num_blocks(h)
+            if w == 1 and h == 1:
+                break
+            w, h = max(1, w // 2), max(1, h // 2)
+        blocks.append(nb)
+    stream = torch.cuda.Stream()
+
+    def plain_one(k):
+        sd = int(sides[k])
+        f = tx.Format(fmts[k])
+        with torch.cuda.stream(stream):
+            lv = [imgs[k].to("cuda", non_blocking=True)]
+            w = h = sd
+            jobs = []
+            while w > 1 or h > 1:
+                nw, nh = max(1, w // 2), max(1, h // 2)
+                lv.append(torch.empty((nh, nw, 4), dtype=torch.uint8, device="cuda"))
+                w, h = nw, nh
+            for a, b in zip(lv[:-1], lv[1:]):
+                tx.mip_batch_device([(a.data_ptr(), a.shape[1] * 4, a.shape[1], a.shape[0], 4, b.data_ptr(),
+                                      b.shape[1] * 4)], stream.cuda_stream)
+            dout = torch.empty(sizes[k], dtype=torch.uint8, device="cuda")
+            off = 0
+            for img in lv:
+                hh, ww = img.shape[:2]
+                n = f.compressed_size(ww, hh)
+                tx.compress_device(f, img.data_ptr(), ww * 4, 4, ww, hh, params, dout.data_ptr() + off, n,
+                                   stream.cuda_stream)
+                off += n
+            out_plain[k].copy_(dout, non_blocking=True)
+        stream.synchronize()
+        del jobs
+
+    srv = tx.Server(memory_budget=40 << 30)
+    # warm both paths
+    plain_one(0)
+    srv.wait(srv.submit(imgs[0].numpy(), int(sides[0]), int(sides[0]), tx.Format(fmts[0]), params,
+                        out_srv[0].numpy()))
+    torch.cuda.synchronize()
+    res = {}
+    total_blocks = sum(blocks)
+    for rate in rates:
+        gaps = np.random.default_rng(rate).exponential(1.0 / rate, n_req)
+        arrive = np.cumsum(gaps) - gaps[0]
+        # served
+        t0 = time.perf_counter()
+        ids = []
+        for k in range(n_req):
+            while time.perf_counter() - t0 < arrive[k]:
+                pass
+            lag = (time.perf_counter() - t0) - arrive[k]
+            ids.append((srv.submit(imgs[k].numpy(), int(sides[k]), int(sides[k]), tx.Format(fmts[k]), params,
+                                   out_srv[k].numpy()), lag))
+        lat_s = []
+        for rid, lag in ids:
+            r = srv.wait(rid)
+            assert r["status"] == 0
+            lat_s.append(r["latency_us"] * 1e-3 + lag * 1e3)
+        done_s = max(arrive[k] * 1e3 + lat_s[k] for k in range(n_req))
+        # plain, one request at a time in arrival order
+        t0 = time.perf_counter()
+        lat_p, done_p = [], 0.0
+        for k in range(n_req):
+            while time.perf_counter() - t0 < arrive[k]:
+                pass
+            plain_one(k)
+            t = (time.perf_counter() - t0) * 1e3
+            lat_p.append(t - arrive[k] * 1e3)
+            done_p = t
+        same = all(torch.equal(a, b) for a, b in zip(out_srv, out_plain))
+        span_s, span_p = done_s - arrive[0] * 1e3, done_p - arrive[0] * 1e3
+        res[str(rate)] = {
+            "served": {"p50_ms": round(float(np.percentile(lat_s, 50)), 2),
+                       "p99_ms": round(float(np.percentile(lat_s, 99)), 2),
+                       "throughput_req_s": round(n_req / span_s * 1e3, 1),
+                       "mblocks_s": round(total_blocks / span_s / 1e3, 1)},
+            "plain": {"p50_ms": round(float(np.percentile(lat_p, 50)), 2),
+                      "p99_ms": round(float(np.percentile(lat_p, 99)), 2),
+                      "throughput_req_s": round(n_req / span_p * 1e3, 1),
+                      "mblocks_s": round(total_blocks / span_p / 1e3, 1)},
+            "throughput_gain": round(span_p / span_s, 2),
+            "identical_outputs": same,
+        }
+    st = srv.stats()
+    srv.close()
+    return {"requests_per_rate": n_req, "blocks_per_rate": total_blocks, "rates": res,
+            "server": {"steps": st["steps"], "arena_high_water_gb": round(st["arena_high_water"] / 2**30, 2),
+                       "budget_gb": 40},
+            "workload": "RGBA8 side log-uniform 64..8192 + mip chain, BC1/BC3/BC5 IterativeClusterFit, "
+                        "Poisson arrivals"}
+
+
 def run_case(args):
     """One workload, device timing only (used for ncu captures)."""
     import torch
@@ -601,6 +716,12 @@ def main():
         return run_reference(args)
     if args.case:
         return run_case(args)
+    if args.serving_only:
+        import torch
+        import texpresso_gb300 as tx
+        torch.cuda.set_device(0)
+        print(json.dumps({"serving": serving(torch, tx, args)}), flush=True)
+        return 0
     if args.batched_only:
         import torch
         import texpresso_gb300 as tx

@@ -221,6 +221,63 @@ TX_API uint32_t tx_mip_count(uint32_t width, uint32_t height);
 /* Produce one level for every job, stream-ordered, no allocation. */
 TX_API int tx_mip_batch_device(const tx_mip_job *jobs, size_t njobs, void *stream);
 
+/* ---------------------------------------------------------------------------
+ * Serving form (no counterpart in the reference): a request loop that admits
+ * compression jobs while a device-memory budget allows, batches every ready
+ * job into each compression step (continuous batching: jobs that arrive while
+ * others run join the next step; each job gets a round-robin share of every
+ * step) and overlaps host<->device copies with compression.  A job's output
+ * bytes are the same as tx_compress's for every level. */
+
+/* Compressed bytes of a level chain: level 0 only (mips == 0) or every
+ * box-filtered level down to 1x1 (mips != 0), concatenated level 0 first. */
+TX_API size_t tx_chain_compressed_size(int format, uint32_t width, uint32_t height, int mips);
+
+typedef struct tx_server_config {
+    size_t memory_budget;     /* device bytes for admitted jobs (one arena); default 40 GiB */
+    uint32_t step_blocks;     /* blocks per compression step; default 1 Mi */
+    uint32_t min_share;       /* blocks a ready job gets per step at least; default 16 Ki */
+    tx_batch_tuning tuning;   /* launch shape of the step kernels (zero fields: defaults) */
+} tx_server_config;
+
+typedef struct tx_server_request {
+    const uint8_t *rgba;      /* host RGBA8, width*height*4 bytes, valid until the job completes */
+    uint32_t width, height;
+    int32_t format;           /* TX_FORMAT_* */
+    tx_params params;
+    int32_t mips;             /* non-zero: compress the full mip chain */
+    uint8_t *output;          /* host, tx_chain_compressed_size() bytes, written on completion */
+    size_t output_len;
+} tx_server_request;
+
+typedef struct tx_server_result {
+    int32_t status;           /* TX_OK or the error that ended the job */
+    uint32_t levels, steps;   /* levels compressed, compression steps the job took part in */
+    uint64_t blocks;
+    double latency_us;        /* submit -> output written to host */
+    double queue_us;          /* submit -> admitted into device memory */
+} tx_server_result;
+
+typedef struct tx_server_stats {
+    uint64_t submitted, completed, steps;
+    size_t arena_bytes, arena_high_water;
+} tx_server_stats;
+
+typedef struct tx_server tx_server;
+
+TX_API void tx_server_default_config(tx_server_config *config);
+/* Allocate the arena and start the worker thread on the current device. */
+TX_API int tx_server_create(const tx_server_config *config, tx_server **server);
+/* Queue a job (thread-safe).  A job larger than the whole budget returns
+ * TX_ERR_OUT_OF_MEMORY at once. */
+TX_API int tx_server_submit(tx_server *server, const tx_server_request *request, uint64_t *id);
+/* Wait for a job (timeout_ms < 0: no limit) and release it; returns the
+ * job's status, or TX_ERR_TIMEOUT with the job still pending. */
+TX_API int tx_server_wait(tx_server *server, uint64_t id, int timeout_ms, tx_server_result *result);
+TX_API int tx_server_get_stats(tx_server *server, tx_server_stats *stats);
+/* Finish every queued job, then stop the worker and free the arena. */
+TX_API void tx_server_destroy(tx_server *server);
+
 /* The CUDA error behind the last TX_ERR_CUDA returned on this thread
  * (a cudaError_t value), or 0. */
 TX_API int tx_last_cuda_error(void);

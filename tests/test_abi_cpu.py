@@ -122,3 +122,15 @@ def test_mip_reference_definition():
     assert m.shape == (1, 2, 4)
     a = img.astype(int)
     assert m[0, 1, 0] == (a[0, 2, 0] + a[0, 3, 0] + a[1, 2, 0] + a[1, 3, 0] + 2) >> 2
+
+
+def test_server_needs_a_device(tx):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    with pytest.raises(tx.TexpressoError) as e:
+        tx.Server(memory_budget=1 << 20)
+    assert e.value.status == -6
+    assert tx.chain_compressed_size(0, 4, 4, False) == 8
+    assert tx.chain_compressed_size(0, 8, 8, True) == 8 * 4 + 8 + 8 + 8  # 8x8, 4x4, 2x2, 1x1
+    assert tx.chain_compressed_size(9, 8, 8, True) == 0

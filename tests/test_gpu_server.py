@@ -1,0 +1,118 @@
+"""Serving form (tx_server_*): jobs admitted by device memory, continuously
+batched into shared compression steps.  Every job's bytes must equal the
+oracle's per level, be the same alone and in a mix, and survive a budget
+that forces jobs to queue for memory."""
+import threading
+
+import numpy as np
+import pytest
+
+from texpresso_gb300 import workloads
+
+pytestmark = pytest.mark.gpu
+
+PERCEPTUAL = (0.2126, 0.7152, 0.0722)
+
+
+def _job(seed, side_max=300):
+    rng = np.random.default_rng(seed)
+    w, h = int(rng.integers(1, side_max)), int(rng.integers(1, side_max))
+    fmt = int(rng.integers(0, 5))
+    alg = int(rng.integers(0, 3))
+    aw = bool(rng.integers(0, 2))
+    mips = bool(rng.integers(0, 4))  # mostly with mips
+    img = workloads.ramp_texture(w, h, seed=seed, alpha="ramp")
+    return dict(img=img, w=w, h=h, fmt=fmt, alg=alg, aw=aw, mips=mips)
+
+
+def _expected(oracle, j):
+    out, img = [], j["img"]
+    while True:
+        h, w = img.shape[:2]
+        out.append(oracle.compress(j["fmt"], img, w, h, oracle.make_params(j["alg"], PERCEPTUAL, j["aw"])))
+        if not j["mips"] or (w == 1 and h == 1):
+            break
+        img = workloads.mip_reference(img)
+    return np.concatenate(out)
+
+
+def _submit(tx, srv, j):
+    out = np.zeros(tx.chain_compressed_size(j["fmt"], j["w"], j["h"], j["mips"]), np.uint8)
+    p = tx.Params(algorithm=tx.Algorithm(j["alg"]), weigh_colour_by_alpha=j["aw"])
+    return srv.submit(j["img"], j["w"], j["h"], tx.Format(j["fmt"]), p, out, mips=j["mips"]), out
+
+
+def test_jobs_match_oracle(tx, cuda, oracle):
+    srv = tx.Server(memory_budget=256 << 20, step_blocks=4096, min_share=512)
+    jobs = [_job(s) for s in range(40)]
+    sub = [_submit(tx, srv, j) for j in jobs]
+    for j, (rid, out) in zip(jobs, sub):
+        res = srv.wait(rid, timeout_ms=60000)
+        assert res["status"] == 0
+        assert np.array_equal(out, _expected(oracle, j)), (j["w"], j["h"], j["fmt"], j["alg"], j["mips"])
+    st = srv.stats()
+    assert st["completed"] == 40 and st["steps"] > 0
+    srv.close()
+
+
+def test_same_alone_and_in_a_mix(tx, cuda):
+    target = _job(1234, side_max=520)
+    target["alg"], target["fmt"], target["mips"] = 2, 0, True  # iterative ClusterFit, BC1, mips
+    srv = tx.Server(memory_budget=512 << 20, step_blocks=8192, min_share=1024)
+    rid, alone = _submit(tx, srv, target)
+    r0 = srv.wait(rid, timeout_ms=60000)
+    mix = [_job(s, side_max=520) for s in range(100, 130)]
+    ids = [_submit(tx, srv, j) for j in mix[:15]]
+    rid2, mixed = _submit(tx, srv, target)
+    ids += [_submit(tx, srv, j) for j in mix[15:]]
+    r1 = srv.wait(rid2, timeout_ms=60000)
+    for i, _ in ids:
+        srv.wait(i, timeout_ms=60000)
+    assert r0["status"] == r1["status"] == 0
+    assert r1["steps"] >= r0["steps"]  # it shared steps with the others
+    assert np.array_equal(alone, mixed)
+    srv.close()
+
+
+def test_admission_by_memory_budget(tx, cuda, oracle):
+    jobs = [_job(s, side_max=200) for s in range(500, 530)]
+    for j in jobs:
+        j["mips"] = True
+    biggest = max(j["w"] * j["h"] for j in jobs)
+    budget = 3 * (biggest * 4 * 2 + (1 << 16))  # room for only a few jobs at a time
+    srv = tx.Server(memory_budget=budget, step_blocks=2048, min_share=256)
+    sub = [_submit(tx, srv, j) for j in jobs]
+    queued = 0
+    for j, (rid, out) in zip(jobs, sub):
+        res = srv.wait(rid, timeout_ms=60000)
+        queued += res["queue_us"] > 0
+        assert np.array_equal(out, _expected(oracle, j))
+    st = srv.stats()
+    assert st["arena_high_water"] <= budget
+    # a job that can never fit is refused at once
+    big = np.zeros((1024, 1024, 4), np.uint8)
+    with pytest.raises(tx.TexpressoError) as e:
+        srv.submit(big, 1024, 1024, tx.Format.Bc1, tx.Params(), np.zeros(tx.chain_compressed_size(0, 1024, 1024), np.uint8))
+    assert e.value.status == -8
+    srv.close()
+
+
+def test_submit_from_many_threads(tx, cuda, oracle):
+    srv = tx.Server(memory_budget=256 << 20, step_blocks=4096)
+    jobs = [_job(s, side_max=120) for s in range(900, 948)]
+    results = [None] * len(jobs)
+
+    def run(lo):
+        for k in range(lo, len(jobs), 4):
+            rid, out = _submit(tx, srv, jobs[k])
+            srv.wait(rid, timeout_ms=60000)
+            results[k] = out
+
+    ts = [threading.Thread(target=run, args=(i,)) for i in range(4)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    for j, out in zip(jobs, results):
+        assert np.array_equal(out, _expected(oracle, j))
+    srv.close()

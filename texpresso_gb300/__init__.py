@@ -327,3 +327,103 @@ def mip_batch_device(jobs, stream=0):
         arr[i].src, arr[i].src_pitch, arr[i].width, arr[i].height = src, sp, w, h
         arr[i].channels, arr[i].dst, arr[i].dst_pitch = ch, dst, dp
     _check(_lib.tx_mip_batch_device(arr, len(jobs), stream or None), "tx_mip_batch_device")
+
+
+# ---------------------------------------------------------------------------
+# serving form (tx_server_*)
+
+class ServerConfig(ctypes.Structure):
+    _fields_ = [("memory_budget", _sz), ("step_blocks", ctypes.c_uint32), ("min_share", ctypes.c_uint32),
+                ("tuning", BatchTuning)]
+
+
+class ServerRequest(ctypes.Structure):
+    _fields_ = [("rgba", _vp), ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("format", ctypes.c_int32),
+                ("params", _CParams), ("mips", ctypes.c_int32), ("output", _vp), ("output_len", _sz)]
+
+
+class ServerResult(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("levels", ctypes.c_uint32), ("steps", ctypes.c_uint32),
+                ("blocks", ctypes.c_uint64), ("latency_us", ctypes.c_double), ("queue_us", ctypes.c_double)]
+
+
+class ServerStats(ctypes.Structure):
+    _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("steps", ctypes.c_uint64),
+                ("arena_bytes", _sz), ("arena_high_water", _sz)]
+
+
+_lib.tx_chain_compressed_size.restype = _sz
+_lib.tx_chain_compressed_size.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
+_lib.tx_server_default_config.argtypes = [ctypes.POINTER(ServerConfig)]
+_lib.tx_server_default_config.restype = None
+_lib.tx_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]
+_lib.tx_server_submit.argtypes = [_vp, ctypes.POINTER(ServerRequest), ctypes.POINTER(ctypes.c_uint64)]
+_lib.tx_server_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ServerResult)]
+_lib.tx_server_get_stats.argtypes = [_vp, ctypes.POINTER(ServerStats)]
+_lib.tx_server_destroy.argtypes = [_vp]
+_lib.tx_server_destroy.restype = None
+
+
+def chain_compressed_size(fmt, width, height, mips=True):
+    """Bytes of every compressed level of a mip chain (or of level 0 alone)."""
+    return int(_lib.tx_chain_compressed_size(int(fmt), width, height, 1 if mips else 0))
+
+
+class Server:
+    """Request loop with admission by device memory and continuous batching."""
+
+    def __init__(self, memory_budget=None, step_blocks=None, min_share=None, tuning=None):
+        c = ServerConfig()
+        _lib.tx_server_default_config(ctypes.byref(c))
+        if memory_budget:
+            c.memory_budget = memory_budget
+        if step_blocks:
+            c.step_blocks = step_blocks
+        if min_share:
+            c.min_share = min_share
+        if tuning is not None:
+            c.tuning = tuning
+        h = _vp()
+        _check(_lib.tx_server_create(ctypes.byref(c), ctypes.byref(h)), "tx_server_create")
+        self._h = h
+        self._keep = {}
+
+    def submit(self, rgba, width, height, fmt, params, output, mips=True):
+        """Queue a job; rgba (host RGBA8) and output (host) stay referenced until wait()."""
+        src, slen = _buffer(rgba, False)
+        dst, dlen = _buffer(output, True)
+        if slen < width * height * 4:
+            raise TexpressoError(-4, "Server.submit")
+        r = ServerRequest()
+        r.rgba, r.width, r.height, r.format = src, width, height, int(fmt)
+        r.params, r.mips, r.output, r.output_len = params._c(), 1 if mips else 0, dst, dlen
+        rid = ctypes.c_uint64()
+        _check(_lib.tx_server_submit(self._h, ctypes.byref(r), ctypes.byref(rid)), "tx_server_submit")
+        self._keep[rid.value] = (rgba, output)
+        return rid.value
+
+    def wait(self, rid, timeout_ms=-1):
+        res = ServerResult()
+        rc = _lib.tx_server_wait(self._h, rid, timeout_ms, ctypes.byref(res))
+        if rc != -7:
+            self._keep.pop(rid, None)
+        _check(rc, "tx_server_wait")
+        return {"status": res.status, "levels": res.levels, "steps": res.steps, "blocks": res.blocks,
+                "latency_us": res.latency_us, "queue_us": res.queue_us}
+
+    def stats(self):
+        s = ServerStats()
+        _check(_lib.tx_server_get_stats(self._h, ctypes.byref(s)), "tx_server_get_stats")
+        return {f: int(getattr(s, f)) for f, _ in s._fields_}
+
+    def close(self):
+        if getattr(self, "_h", None):
+            _lib.tx_server_destroy(self._h)
+            self._h = None
+            self._keep.clear()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -22,6 +22,7 @@
 #include "tx_alpha.cuh"
 #include "tx_colour.cuh"
 #include "tx_internal.h"
+#include "tx_batch_internal.h"
 
 #include <algorithm>
 #include <chrono>
@@ -31,26 +32,6 @@
 #include <vector>
 
 namespace tx {
-
-enum UnitKind : int32_t { KIND_ALPHA = 0, KIND_RANGE = 1, KIND_CLUSTER = 2, KIND_CLUSTER_ITER = 3 };
-
-struct BatchItem {
-    SrcDesc src;
-    DevParams prm;
-    uint8_t *dst;
-    uint32_t nblocks;
-    int32_t format;
-    int32_t kind;
-    int32_t channels;
-};
-
-struct BatchQueue {
-    const BatchItem *items;
-    const uint2 *units;     // (item, first block)
-    uint32_t nunits;
-    uint32_t *counter;
-    uint32_t per_unit;      // lane units: blocks per lane; team units: blocks per unit
-};
 
 cudaError_t upload_batch_tables(const uint32_t lut[4][256][2]) { return upload_tables_this_tu(lut); }
 
@@ -326,7 +307,7 @@ int tx_mip_batch_device(const tx_mip_job *jobs, size_t njobs, void *stream) {
         const tx_mip_job &j = jobs[i];
         if (!j.src || !j.dst || j.width == 0 || j.height == 0) return TX_ERR_INVALID_ARGUMENT;
         if (j.channels < 1 || j.channels > 4) return TX_ERR_INVALID_ARGUMENT;
-        const uint32_t dw = j.width > 1 ? j.width >> 1 : 1, dh = j.height > 1 ? j.height >> 1 : 1;
+        const uint32_t dw = j.width > 1 ? j.width >> 1 : 1;
         if (j.src_pitch < (size_t)j.width * j.channels || j.dst_pitch < (size_t)dw * j.channels)
             return TX_ERR_INVALID_ARGUMENT;
         if (j.src_pitch > 0xFFFFFFFFu || j.dst_pitch > 0xFFFFFFFFu) return TX_ERR_INVALID_ARGUMENT;
@@ -750,3 +731,70 @@ extern "C" int tx_batch_launch_noalloc(const tx_batch_item *items, size_t nitems
     }
     return TX_OK;
 }
+
+// ===========================================================================
+// helpers for the serving loop (tx_server.cu)
+
+namespace tx {
+
+void fill_batch_item(const tx_batch_item &it, BatchItem *d) {
+    std::memset(d, 0, sizeof(*d));
+    d->src.base = static_cast<const uint8_t *>(it.src);
+    d->src.pitch = it.src_pitch;
+    d->src.width = it.width;
+    d->src.height = it.height;
+    d->src.blocks_wide = (uint32_t)tx_num_blocks(it.width);
+    d->src.channels = it.channels;
+    const size_t va = it.channels == 4 ? 16 : (size_t)it.channels * 4;
+    d->src.vec16 = ((reinterpret_cast<uintptr_t>(it.src) % va) == 0 && (it.src_pitch % va) == 0) ? 1 : 0;
+    for (int c = 0; c < 3; ++c) d->prm.w[c] = it.params.weights[c];
+    d->prm.alpha_weighted = it.params.weigh_colour_by_alpha ? 1 : 0;
+    d->dst = static_cast<uint8_t *>(it.dst);
+    d->nblocks = (uint32_t)(tx_num_blocks(it.width) * tx_num_blocks(it.height));
+    d->format = it.format;
+    d->channels = it.channels;
+    const int alg = it.params.algorithm;
+    if (it.format == TX_FORMAT_BC4 || it.format == TX_FORMAT_BC5) d->kind = KIND_ALPHA;
+    else if (alg == TX_RANGE_FIT) d->kind = KIND_RANGE;
+    else d->kind = alg == TX_ITERATIVE_CLUSTER_FIT ? KIND_CLUSTER_ITER : KIND_CLUSTER;
+}
+
+cudaError_t launch_batch_queues(const BatchItem *d_items, const uint2 *d_lane, uint32_t n_lane,
+                                uint32_t lane_blocks_per_lane, const uint2 *d_team, uint32_t n_team,
+                                uint32_t team_blocks_per_unit, uint32_t *d_counters, int sm_count,
+                                const tx_batch_tuning &t, cudaStream_t st) {
+    if (n_lane) {
+        uint32_t grid = (uint32_t)(sm_count * t.lane_ctas_per_sm);
+        grid = std::max<uint32_t>(1, std::min<uint32_t>(grid, (n_lane + 3) / 4));
+        BatchQueue q{d_items, d_lane, n_lane, d_counters, lane_blocks_per_lane};
+        k_batch_lanes<<<grid, 128, 0, st>>>(q);
+        note_launch();
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) return e;
+    }
+    if (n_team) {
+        const int threads = t.team_threads_per_cta;
+        const int team = t.team_lanes == 16 ? 16 : 32;
+        uint32_t grid = (uint32_t)(sm_count * t.team_ctas_per_sm);
+        const uint32_t per = (uint32_t)(threads / team);
+        grid = std::max<uint32_t>(1, std::min<uint32_t>(grid, (n_team + per - 1) / per));
+        BatchQueue q{d_items, d_team, n_team, d_counters + 1, team_blocks_per_unit};
+        cudaError_t e;
+        if (team == 16) {
+            e = cudaFuncSetAttribute(k_batch_teams<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)cluster_smem_bytes(16, 1024));
+            if (e != cudaSuccess) return e;
+            k_batch_teams<16><<<grid, threads, cluster_smem_bytes(16, threads), st>>>(q);
+        } else {
+            e = cudaFuncSetAttribute(k_batch_teams<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)cluster_smem_bytes(32, 1024));
+            if (e != cudaSuccess) return e;
+            k_batch_teams<32><<<grid, threads, cluster_smem_bytes(32, threads), st>>>(q);
+        }
+        note_launch();
+        if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
+}  // namespace tx

@@ -1,0 +1,602 @@
+// tx_server.cu -- serving form: a request loop with admission by device memory
+// and continuous batching.
+//
+// A server owns one device-memory arena (the admission budget), three streams
+// (host->device copies and mip generation, compression steps, device->host
+// copies) and one worker thread.  Requests are admitted first-in first-out as
+// arena space frees up; an admitted request's pixels are copied in and its mip
+// chain built on the copy stream, overlapping the running compression steps.
+// Every step is one launch of the persistent batch kernels over a work queue
+// assembled from all ready requests: each gets a round-robin share of blocks,
+// so requests that arrive while others run join the very next step and small
+// requests finish without waiting for large ones.  Two steps are kept in
+// flight; the queue of step n+1 is written while step n runs.  When a request's
+// last blocks have been compressed its levels are copied back on the third
+// stream and its arena space is released.
+//
+// Each block is encoded by the same per-block code as every other entry point,
+// so a request's bytes do not depend on what else is in flight.
+#include "texpresso_gb300.h"
+#include "tx_batch_internal.h"
+#include "tx_internal.h"
+
+#include <algorithm>
+#include <atomic>
+#include <chrono>
+#include <condition_variable>
+#include <cstring>
+#include <deque>
+#include <map>
+#include <mutex>
+#include <new>
+#include <thread>
+#include <unordered_map>
+#include <vector>
+
+namespace {
+
+double now_us() {
+    using namespace std::chrono;
+    return (double)duration_cast<nanoseconds>(steady_clock::now().time_since_epoch()).count() * 1e-3;
+}
+
+constexpr size_t kAlign = 256;
+size_t align_up(size_t v) { return (v + kAlign - 1) & ~(kAlign - 1); }
+
+// First-fit allocator over [0, size) with coalescing frees.
+class Arena {
+  public:
+    void reset(size_t size) {
+        free_.clear();
+        if (size) free_[0] = size;
+        used_ = 0;
+        high_ = 0;
+    }
+    bool alloc(size_t n, size_t *off) {
+        for (auto it = free_.begin(); it != free_.end(); ++it) {
+            if (it->second >= n) {
+                *off = it->first;
+                const size_t rest = it->second - n, start = it->first + n;
+                free_.erase(it);
+                if (rest) free_[start] = rest;
+                used_ += n;
+                high_ = std::max(high_, used_);
+                return true;
+            }
+        }
+        return false;
+    }
+    void release(size_t off, size_t n) {
+        used_ -= n;
+        auto it = free_.emplace(off, n).first;
+        auto next = std::next(it);
+        if (next != free_.end() && it->first + it->second == next->first) {
+            it->second += next->second;
+            free_.erase(next);
+        }
+        if (it != free_.begin()) {
+            auto prev = std::prev(it);
+            if (prev->first + prev->second == it->first) {
+                prev->second += it->second;
+                free_.erase(it);
+            }
+        }
+    }
+    size_t high() const { return high_; }
+
+  private:
+    std::map<size_t, size_t> free_;
+    size_t used_ = 0, high_ = 0;
+};
+
+struct Level {
+    uint32_t w, h, nblocks;
+    size_t src_off, dst_off, dst_bytes, out_off;
+};
+
+struct Request {
+    uint64_t id = 0;
+    tx_server_request r{};
+    std::vector<Level> levels;
+    size_t footprint = 0, arena_off = 0;
+    enum State { QUEUED, LOADING, ACTIVE, DRAINING, DONE } state = QUEUED;
+    std::vector<uint32_t> next_block;
+    size_t unassigned = 0;
+    cudaEvent_t ready_ev = nullptr, done_ev = nullptr;
+    double t_submit = 0, t_admit = 0, t_done = 0;
+    int status = TX_OK;
+    uint32_t steps = 0;
+    std::atomic<bool> finished{false};  // set under tx_server::mu; read by waiters
+};
+
+struct Step {
+    tx::BatchItem *d_items = nullptr;
+    uint2 *d_units = nullptr;
+    uint32_t *d_counters = nullptr;
+    tx::BatchItem *h_items = nullptr;  // pinned staging
+    uint2 *h_units = nullptr;          // pinned staging
+    cudaEvent_t done = nullptr;
+    std::vector<Request *> finishing;
+    bool busy = false;
+};
+
+}  // namespace
+
+struct tx_server {
+    tx_server_config cfg{};
+    int device = 0, sm_count = 0;
+    uint8_t *arena_base = nullptr;
+    Arena arena;
+    cudaStream_t s_load = nullptr, s_comp = nullptr, s_store = nullptr;
+    Step steps[2];
+    uint32_t max_items = 0, max_units = 0;
+    uint64_t step_count = 0;
+    int next_step = 0;
+
+    std::mutex mu;
+    std::condition_variable cv_work, cv_done;
+    std::deque<Request *> submitted;                   // guarded by mu
+    std::unordered_map<uint64_t, Request *> requests;  // guarded by mu
+    uint64_t next_id = 1;
+    bool stopping = false;
+    int fatal = TX_OK;
+    uint64_t n_submitted = 0, n_completed = 0;
+
+    std::deque<Request *> waiting;   // worker only: not yet admitted
+    std::vector<Request *> live;     // worker only: admitted, not done
+    size_t rr = 0;                   // round-robin cursor
+    std::thread worker;
+};
+
+namespace {
+
+int fail_server(cudaError_t e) {
+    tx_internal_set_last_cuda_error((int)e);
+    return e == cudaErrorMemoryAllocation ? TX_ERR_OUT_OF_MEMORY : TX_ERR_CUDA;
+}
+
+void plan_levels(Request *q) {
+    const tx_server_request &r = q->r;
+    uint32_t w = r.width, h = r.height;
+    const uint32_t n = r.mips ? tx_mip_count(w, h) : 1;
+    size_t off = 0, out = 0;
+    for (uint32_t l = 0; l < n; ++l) {
+        Level lv;
+        lv.w = w;
+        lv.h = h;
+        lv.nblocks = (uint32_t)(tx_num_blocks(w) * tx_num_blocks(h));
+        lv.src_off = off;
+        off += align_up((size_t)w * h * 4);
+        lv.dst_bytes = tx_compressed_size(r.format, w, h);
+        lv.out_off = out;
+        out += lv.dst_bytes;
+        q->levels.push_back(lv);
+        w = w > 1 ? w >> 1 : 1;
+        h = h > 1 ? h >> 1 : 1;
+    }
+    for (Level &lv : q->levels) {
+        lv.dst_off = off;
+        off += align_up(lv.dst_bytes);
+    }
+    q->footprint = off;
+    q->next_block.assign(q->levels.size(), 0);
+    for (const Level &lv : q->levels) q->unassigned += lv.nblocks;
+}
+
+// Admit the head of the waiting line while arena space lasts (FIFO).
+int admit(tx_server *s) {
+    while (!s->waiting.empty()) {
+        Request *q = s->waiting.front();
+        size_t off = 0;
+        if (!s->arena.alloc(q->footprint, &off)) break;
+        s->waiting.pop_front();
+        q->arena_off = off;
+        q->t_admit = now_us();
+        q->state = Request::LOADING;
+        uint8_t *base = s->arena_base + off;
+        const Level &l0 = q->levels[0];
+        cudaError_t e = cudaMemcpyAsync(base + l0.src_off, q->r.rgba, (size_t)l0.w * l0.h * 4, cudaMemcpyHostToDevice,
+                                        s->s_load);
+        if (e != cudaSuccess) return fail_server(e);
+        for (size_t l = 1; l < q->levels.size(); ++l) {
+            const Level &a = q->levels[l - 1], &b = q->levels[l];
+            tx_mip_job job{base + a.src_off, (size_t)a.w * 4, a.w, a.h, 4, base + b.src_off, (size_t)b.w * 4};
+            int rc = tx_mip_batch_device(&job, 1, s->s_load);
+            if (rc != TX_OK) return rc;
+        }
+        if ((e = cudaEventRecord(q->ready_ev, s->s_load)) != cudaSuccess) return fail_server(e);
+        s->live.push_back(q);
+    }
+    return TX_OK;
+}
+
+// Assemble one step from the ready requests and enqueue it.
+int schedule_step(tx_server *s) {
+    Step &st = s->steps[s->next_step];
+    if (st.busy) return TX_OK;
+    std::vector<Request *> ready;
+    for (Request *q : s->live)
+        if (q->state == Request::ACTIVE && q->unassigned > 0) ready.push_back(q);
+    if (ready.empty()) return TX_OK;
+    const uint32_t cap = s->cfg.step_blocks;
+    const size_t share = std::max<size_t>(s->cfg.min_share, cap / ready.size());
+    uint32_t n_items = 0, n_lane = 0, n_team_iter = 0, n_team = 0;
+    std::vector<uint2> lane_units, iter_units, team_units;
+    const uint32_t lane_span = 32u * (uint32_t)s->cfg.tuning.lane_blocks_per_lane;
+    const uint32_t team_span = (uint32_t)s->cfg.tuning.team_blocks_per_unit;
+    size_t budget = cap;
+    st.finishing.clear();
+    const size_t start = s->rr % ready.size();
+    for (size_t k = 0; k < ready.size() && budget > 0 && n_items < s->max_items; ++k) {
+        Request *q = ready[(start + k) % ready.size()];
+        size_t take = std::min(share, budget);
+        for (size_t l = 0; l < q->levels.size() && take > 0 && n_items < s->max_items; ++l) {
+            Level &lv = q->levels[l];
+            uint32_t &nb = q->next_block[l];
+            if (nb >= lv.nblocks) continue;
+            const uint32_t n = (uint32_t)std::min<size_t>(take, lv.nblocks - nb);
+            tx_batch_item it{};
+            it.src = s->arena_base + q->arena_off + lv.src_off;
+            it.src_pitch = (size_t)lv.w * 4;
+            it.width = lv.w;
+            it.height = lv.h;
+            it.format = q->r.format;
+            it.channels = 4;
+            it.params = q->r.params;
+            it.dst = s->arena_base + q->arena_off + lv.dst_off;
+            tx::fill_batch_item(it, &st.h_items[n_items]);
+            const tx::BatchItem &d = st.h_items[n_items];
+            const bool lane = d.kind == tx::KIND_ALPHA || d.kind == tx::KIND_RANGE;
+            const uint32_t span = lane ? lane_span : team_span;
+            auto &dst = lane ? lane_units : (d.kind == tx::KIND_CLUSTER_ITER ? iter_units : team_units);
+            for (uint32_t f = nb; f < nb + n; f += span) dst.push_back(make_uint2(n_items, f));
+            // a unit may run past this step's share; the kernels stop at the level's end,
+            // so round the share up to whole units
+            const uint32_t done = std::min<uint32_t>(lv.nblocks - nb, ((n + span - 1) / span) * span);
+            nb += done;
+            q->unassigned -= done;
+            take -= std::min<size_t>(take, done);
+            budget -= std::min<size_t>(budget, done);
+            ++n_items;
+        }
+        q->steps++;
+        if (q->unassigned == 0) st.finishing.push_back(q);
+    }
+    s->rr = start + 1;
+    n_lane = (uint32_t)lane_units.size();
+    n_team_iter = (uint32_t)iter_units.size();
+    n_team = (uint32_t)team_units.size();
+    const uint32_t total = n_lane + n_team_iter + n_team;
+    if (total > s->max_units) return TX_ERR_INVALID_ARGUMENT;  // cannot happen: units <= step_blocks + items
+    std::memcpy(st.h_units, lane_units.data(), n_lane * sizeof(uint2));
+    std::memcpy(st.h_units + n_lane, iter_units.data(), n_team_iter * sizeof(uint2));
+    std::memcpy(st.h_units + n_lane + n_team_iter, team_units.data(), n_team * sizeof(uint2));
+    cudaError_t e;
+    if ((e = cudaMemcpyAsync(st.d_items, st.h_items, n_items * sizeof(tx::BatchItem), cudaMemcpyHostToDevice,
+                             s->s_comp)) != cudaSuccess)
+        return fail_server(e);
+    if ((e = cudaMemcpyAsync(st.d_units, st.h_units, total * sizeof(uint2), cudaMemcpyHostToDevice, s->s_comp)) !=
+        cudaSuccess)
+        return fail_server(e);
+    if ((e = cudaMemsetAsync(st.d_counters, 0, 2 * sizeof(uint32_t), s->s_comp)) != cudaSuccess) return fail_server(e);
+    if ((e = tx::launch_batch_queues(st.d_items, st.d_units, n_lane, lane_span / 32, st.d_units + n_lane,
+                                     n_team_iter + n_team, team_span, st.d_counters, s->sm_count, s->cfg.tuning,
+                                     s->s_comp)) != cudaSuccess)
+        return fail_server(e);
+    if ((e = cudaEventRecord(st.done, s->s_comp)) != cudaSuccess) return fail_server(e);
+    st.busy = true;
+    s->next_step ^= 1;
+    s->step_count++;
+    return TX_OK;
+}
+
+// Retire finished steps: start the device->host copies of requests that are complete.
+int retire_steps(tx_server *s) {
+    for (int i = 0; i < 2; ++i) {
+        Step &st = s->steps[(s->next_step + i) & 1];  // oldest first
+        if (!st.busy) continue;
+        cudaError_t e = cudaEventQuery(st.done);
+        if (e == cudaErrorNotReady) return TX_OK;  // steps complete in order
+        if (e != cudaSuccess) return fail_server(e);
+        for (Request *q : st.finishing) {
+            uint8_t *base = s->arena_base + q->arena_off;
+            if ((e = cudaStreamWaitEvent(s->s_store, st.done, 0)) != cudaSuccess) return fail_server(e);
+            for (const Level &lv : q->levels) {
+                if (lv.dst_bytes == 0) continue;
+                if ((e = cudaMemcpyAsync(q->r.output + lv.out_off, base + lv.dst_off, lv.dst_bytes, cudaMemcpyDeviceToHost,
+                                         s->s_store)) != cudaSuccess)
+                    return fail_server(e);
+            }
+            if ((e = cudaEventRecord(q->done_ev, s->s_store)) != cudaSuccess) return fail_server(e);
+            q->state = Request::DRAINING;
+        }
+        st.finishing.clear();
+        st.busy = false;
+    }
+    return TX_OK;
+}
+
+// Promote loaded requests and complete drained ones.
+int progress(tx_server *s, bool *completed_any) {
+    *completed_any = false;
+    for (size_t i = 0; i < s->live.size();) {
+        Request *q = s->live[i];
+        if (q->state == Request::LOADING) {
+            cudaError_t e = cudaEventQuery(q->ready_ev);
+            if (e == cudaSuccess) {
+                q->state = Request::ACTIVE;
+                if (q->unassigned == 0) {  // an empty image: nothing to compress
+                    q->state = Request::DRAINING;
+                    if ((e = cudaEventRecord(q->done_ev, s->s_load)) != cudaSuccess) return fail_server(e);
+                }
+            } else if (e != cudaErrorNotReady) {
+                return fail_server(e);
+            }
+        } else if (q->state == Request::DRAINING) {
+            cudaError_t e = cudaEventQuery(q->done_ev);
+            if (e == cudaSuccess) {
+                s->arena.release(q->arena_off, q->footprint);
+                std::lock_guard<std::mutex> lk(s->mu);
+                q->t_done = now_us();
+                q->state = Request::DONE;
+                q->finished.store(true);
+                s->n_completed++;
+                s->live.erase(s->live.begin() + (long)i);
+                *completed_any = true;
+                continue;
+            } else if (e != cudaErrorNotReady) {
+                return fail_server(e);
+            }
+        }
+        ++i;
+    }
+    return TX_OK;
+}
+
+void fail_all(tx_server *s, int rc) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    s->fatal = rc;
+    for (auto &kv : s->requests) {
+        Request *q = kv.second;
+        if (!q->finished.load()) {
+            q->status = rc;
+            q->t_done = now_us();
+            q->finished.store(true);
+        }
+    }
+    s->submitted.clear();
+    s->cv_done.notify_all();
+}
+
+void worker_main(tx_server *s) {
+    cudaSetDevice(s->device);
+    for (;;) {
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            if (s->fatal != TX_OK) return;
+            if (s->submitted.empty() && s->waiting.empty() && s->live.empty()) {
+                if (s->stopping) return;
+                s->cv_work.wait_for(lk, std::chrono::milliseconds(5));
+            }
+            while (!s->submitted.empty()) {
+                s->waiting.push_back(s->submitted.front());
+                s->submitted.pop_front();
+            }
+        }
+        int rc = admit(s);
+        bool done = false;
+        if (rc == TX_OK) rc = progress(s, &done);
+        if (rc == TX_OK) rc = retire_steps(s);
+        if (rc == TX_OK) rc = schedule_step(s);
+        if (rc == TX_OK) rc = schedule_step(s);  // keep two steps in flight
+        if (rc != TX_OK) {
+            fail_all(s, rc);
+            return;
+        }
+        if (done) s->cv_done.notify_all();
+        // nothing to launch: let the GPU work before polling again
+        if (s->steps[0].busy && s->steps[1].busy) std::this_thread::sleep_for(std::chrono::microseconds(20));
+        else if (!s->live.empty()) std::this_thread::sleep_for(std::chrono::microseconds(5));
+    }
+}
+
+void destroy_resources(tx_server *s) {
+    for (Step &st : s->steps) {
+        cudaFree(st.d_items);
+        cudaFree(st.d_units);
+        cudaFree(st.d_counters);
+        cudaFreeHost(st.h_items);
+        cudaFreeHost(st.h_units);
+        if (st.done) cudaEventDestroy(st.done);
+    }
+    cudaFree(s->arena_base);
+    if (s->s_load) cudaStreamDestroy(s->s_load);
+    if (s->s_comp) cudaStreamDestroy(s->s_comp);
+    if (s->s_store) cudaStreamDestroy(s->s_store);
+}
+
+}  // namespace
+
+extern "C" {
+
+size_t tx_chain_compressed_size(int format, uint32_t width, uint32_t height, int mips) {
+    if (tx_block_size(format) == 0) return 0;
+    const uint32_t n = mips ? tx_mip_count(width, height) : (width && height ? 1u : 0u);
+    size_t total = 0;
+    for (uint32_t l = 0; l < n; ++l) {
+        total += tx_compressed_size(format, width, height);
+        width = width > 1 ? width >> 1 : 1;
+        height = height > 1 ? height >> 1 : 1;
+    }
+    return total;
+}
+
+void tx_server_default_config(tx_server_config *c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->memory_budget = (size_t)40 << 30;
+    c->step_blocks = 1u << 20;
+    c->min_share = 1u << 14;
+    tx_batch_default_tuning(&c->tuning);
+}
+
+int tx_server_create(const tx_server_config *config, tx_server **out) {
+    if (!out) return TX_ERR_INVALID_ARGUMENT;
+    *out = nullptr;
+    tx_server_config cfg;
+    tx_server_default_config(&cfg);
+    if (config) {
+        if (config->memory_budget) cfg.memory_budget = config->memory_budget;
+        if (config->step_blocks) cfg.step_blocks = config->step_blocks;
+        if (config->min_share) cfg.min_share = config->min_share;
+        tx_batch_tuning t = cfg.tuning;
+        const tx_batch_tuning &u = config->tuning;
+        if (u.team_lanes == 16 || u.team_lanes == 32) t.team_lanes = u.team_lanes;
+        if (u.team_threads_per_cta >= 64 && u.team_threads_per_cta <= 256 && u.team_threads_per_cta % 32 == 0)
+            t.team_threads_per_cta = u.team_threads_per_cta;
+        if (u.team_ctas_per_sm >= 1 && u.team_ctas_per_sm <= 16) t.team_ctas_per_sm = u.team_ctas_per_sm;
+        if (u.team_blocks_per_unit >= 1 && u.team_blocks_per_unit <= 64) t.team_blocks_per_unit = u.team_blocks_per_unit;
+        if (u.lane_ctas_per_sm >= 1 && u.lane_ctas_per_sm <= 16) t.lane_ctas_per_sm = u.lane_ctas_per_sm;
+        if (u.lane_blocks_per_lane >= 1 && u.lane_blocks_per_lane <= 64) t.lane_blocks_per_lane = u.lane_blocks_per_lane;
+        cfg.tuning = t;
+    }
+    if (cfg.step_blocks < 1024 || cfg.step_blocks > (1u << 26)) return TX_ERR_INVALID_ARGUMENT;
+    int rc = tx_internal_ensure_device();
+    if (rc != TX_OK) return rc;
+    tx_server *s = new (std::nothrow) tx_server();
+    if (!s) return TX_ERR_OUT_OF_MEMORY;
+    s->cfg = cfg;
+    cudaGetDevice(&s->device);
+    cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
+    s->max_items = 65536;
+    s->max_units = cfg.step_blocks + s->max_items * 2;
+    cudaError_t e = cudaMalloc(&s->arena_base, cfg.memory_budget);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s_load, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s_comp, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s_store, cudaStreamNonBlocking);
+    for (Step &st : s->steps) {
+        if (e == cudaSuccess) e = cudaMalloc(&st.d_items, s->max_items * sizeof(tx::BatchItem));
+        if (e == cudaSuccess) e = cudaMalloc(&st.d_units, s->max_units * sizeof(uint2));
+        if (e == cudaSuccess) e = cudaMalloc(&st.d_counters, 2 * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMallocHost(&st.h_items, s->max_items * sizeof(tx::BatchItem));
+        if (e == cudaSuccess) e = cudaMallocHost(&st.h_units, s->max_units * sizeof(uint2));
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming);
+    }
+    if (e != cudaSuccess) {
+        destroy_resources(s);
+        delete s;
+        return fail_server(e);
+    }
+    s->arena.reset(cfg.memory_budget);
+    s->worker = std::thread(worker_main, s);
+    *out = s;
+    return TX_OK;
+}
+
+int tx_server_submit(tx_server *s, const tx_server_request *req, uint64_t *id) {
+    if (!s || !req || !id) return TX_ERR_INVALID_ARGUMENT;
+    if (tx_block_size(req->format) == 0) return TX_ERR_INVALID_FORMAT;
+    if (req->params.algorithm < TX_RANGE_FIT || req->params.algorithm > TX_ITERATIVE_CLUSTER_FIT)
+        return TX_ERR_INVALID_ARGUMENT;
+    if (req->width == 0 || req->height == 0 || !req->rgba) return TX_ERR_INVALID_ARGUMENT;
+    if (req->output_len < tx_chain_compressed_size(req->format, req->width, req->height, req->mips))
+        return TX_ERR_OUTPUT_TOO_SMALL;
+    if (!req->output) return TX_ERR_INVALID_ARGUMENT;
+    Request *q = new (std::nothrow) Request();
+    if (!q) return TX_ERR_OUT_OF_MEMORY;
+    q->r = *req;
+    plan_levels(q);
+    if (q->footprint > s->cfg.memory_budget) {
+        delete q;
+        return TX_ERR_OUT_OF_MEMORY;  // could never be admitted
+    }
+    if (cudaEventCreateWithFlags(&q->ready_ev, cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&q->done_ev, cudaEventDisableTiming) != cudaSuccess) {
+        if (q->ready_ev) cudaEventDestroy(q->ready_ev);
+        delete q;
+        return TX_ERR_CUDA;
+    }
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (s->fatal != TX_OK) {
+            cudaEventDestroy(q->ready_ev);
+            cudaEventDestroy(q->done_ev);
+            delete q;
+            return s->fatal;
+        }
+        if (s->stopping) {
+            cudaEventDestroy(q->ready_ev);
+            cudaEventDestroy(q->done_ev);
+            delete q;
+            return TX_ERR_CANCELLED;
+        }
+        q->id = s->next_id++;
+        q->t_submit = now_us();
+        s->requests[q->id] = q;
+        s->submitted.push_back(q);
+        s->n_submitted++;
+        *id = q->id;
+    }
+    s->cv_work.notify_one();
+    return TX_OK;
+}
+
+int tx_server_wait(tx_server *s, uint64_t id, int timeout_ms, tx_server_result *res) {
+    if (!s) return TX_ERR_INVALID_ARGUMENT;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->requests.find(id);
+    if (it == s->requests.end()) return TX_ERR_INVALID_ARGUMENT;
+    Request *q = it->second;
+    auto pred = [&] { return q->finished.load(); };
+    if (timeout_ms < 0) s->cv_done.wait(lk, pred);
+    else if (!s->cv_done.wait_for(lk, std::chrono::milliseconds(timeout_ms), pred)) return TX_ERR_TIMEOUT;
+    if (res) {
+        res->status = q->status;
+        res->latency_us = q->t_done - q->t_submit;
+        res->queue_us = q->t_admit > 0 ? q->t_admit - q->t_submit : q->t_done - q->t_submit;
+        res->blocks = 0;
+        for (const Level &lv : q->levels) res->blocks += lv.nblocks;
+        res->levels = (uint32_t)q->levels.size();
+        res->steps = q->steps;
+    }
+    const int status = q->status;
+    s->requests.erase(it);
+    lk.unlock();
+    cudaEventDestroy(q->ready_ev);
+    cudaEventDestroy(q->done_ev);
+    delete q;
+    return status;
+}
+
+int tx_server_get_stats(tx_server *s, tx_server_stats *out) {
+    if (!s || !out) return TX_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    out->submitted = s->n_submitted;
+    out->completed = s->n_completed;
+    out->steps = s->step_count;
+    out->arena_bytes = s->cfg.memory_budget;
+    out->arena_high_water = s->arena.high();
+    return TX_OK;
+}
+
+void tx_server_destroy(tx_server *s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stopping = true;
+    }
+    s->cv_work.notify_all();
+    if (s->worker.joinable()) s->worker.join();
+    cudaStreamSynchronize(s->s_load);
+    cudaStreamSynchronize(s->s_comp);
+    cudaStreamSynchronize(s->s_store);
+    for (auto &kv : s->requests) {
+        cudaEventDestroy(kv.second->ready_ev);
+        cudaEventDestroy(kv.second->done_ev);
+        delete kv.second;
+    }
+    destroy_resources(s);
+    delete s;
+}
+
+}  // extern "C"
