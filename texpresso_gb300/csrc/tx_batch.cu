@@ -74,7 +74,9 @@ __global__ void __launch_bounds__(256) k_batch_teams(BatchQueue q) {
 __global__ void __launch_bounds__(128) k_batch_lanes(BatchQueue q) {
     __shared__ float s_unorm[256];
     __shared__ float s_sqrt[17];
+    __shared__ float4 s_pts[16 * 128];
     init_unorm_tables(s_unorm, s_sqrt);
+    const PointCol pt{s_pts + threadIdx.x, 128};
     const int lane = threadIdx.x & 31;
     for (;;) {
         uint32_t u = 0;
@@ -91,9 +93,9 @@ __global__ void __launch_bounds__(128) k_batch_lanes(BatchQueue q) {
             const uint32_t b = unit.y + 32u * k + (uint32_t)lane;
             if (b >= it.nblocks) break;
             if (kind == KIND_RANGE) {
-                if (fmt == BC1) range_block<BC1>(src, b, prm, dst, s_unorm, s_sqrt);
-                else if (fmt == BC2) range_block<BC2>(src, b, prm, dst, s_unorm, s_sqrt);
-                else range_block<BC3>(src, b, prm, dst, s_unorm, s_sqrt);
+                if (fmt == BC1) range_block<BC1>(src, b, prm, dst, s_unorm, s_sqrt, pt);
+                else if (fmt == BC2) range_block<BC2>(src, b, prm, dst, s_unorm, s_sqrt, pt);
+                else range_block<BC3>(src, b, prm, dst, s_unorm, s_sqrt, pt);
             } else if (fmt == BC4) {
                 if (ch == 1) alpha_block<BC4, 1>(src, b, dst);
                 else alpha_block<BC4, 4>(src, b, dst);
@@ -235,7 +237,7 @@ cudaError_t launch_teams(tx_batch *b, cudaStream_t st) {
     static bool attr_set[64][2] = {};
     if (b->device < 64 && !attr_set[b->device][TEAM == 16]) {
         cudaError_t e = cudaFuncSetAttribute(tx::k_batch_teams<TEAM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)tx::cluster_smem_bytes(TEAM, 1024));
+                                             (int)tx::cluster_smem_bytes(TEAM, 256));
         if (e != cudaSuccess) return e;
         attr_set[b->device][TEAM == 16] = true;
     }
@@ -614,7 +616,7 @@ int noalloc_setup_device(int dev, NoallocDevice **out) {
         if ((e = cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
             return fail_batch(e);
         if ((e = cudaFuncSetAttribute(tx::k_batch_teams<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)tx::cluster_smem_bytes(32, 1024))) != cudaSuccess)
+                                      (int)tx::cluster_smem_bytes(32, 256))) != cudaSuccess)
             return fail_batch(e);
         d.scratch = static_cast<unsigned char *>(ptr);
         d.ready = true;
@@ -782,12 +784,12 @@ cudaError_t launch_batch_queues(const BatchItem *d_items, const uint2 *d_lane, u
         cudaError_t e;
         if (team == 16) {
             e = cudaFuncSetAttribute(k_batch_teams<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)cluster_smem_bytes(16, 1024));
+                                     (int)cluster_smem_bytes(16, 256));
             if (e != cudaSuccess) return e;
             k_batch_teams<16><<<grid, threads, cluster_smem_bytes(16, threads), st>>>(q);
         } else {
             e = cudaFuncSetAttribute(k_batch_teams<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)cluster_smem_bytes(32, 1024));
+                                     (int)cluster_smem_bytes(32, 256));
             if (e != cudaSuccess) return e;
             k_batch_teams<32><<<grid, threads, cluster_smem_bytes(32, threads), st>>>(q);
         }

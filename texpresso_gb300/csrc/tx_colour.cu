@@ -10,10 +10,12 @@ __global__ void __launch_bounds__(128) k_range(SrcDesc src, DevParams prm, uint8
                                                size_t nblocks) {
     __shared__ float s_unorm[256];
     __shared__ float s_sqrt[17];
+    __shared__ float4 s_pts[16 * 128];
     init_unorm_tables(s_unorm, s_sqrt);
+    const PointCol pt{s_pts + threadIdx.x, 128};
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     for (size_t b = (size_t)blockIdx.x * blockDim.x + threadIdx.x; b < nblocks; b += stride)
-        range_block<FMT>(src, b, prm, out, s_unorm, s_sqrt);
+        range_block<FMT>(src, b, prm, out, s_unorm, s_sqrt, pt);
 }
 
 template <int FMT, int TEAM, int NITER>
@@ -62,7 +64,7 @@ static cudaError_t launch_cluster_t(const SrcDesc &src, const DevParams &prm, ui
     cudaGetDevice(&dev);
     if (dev < 64 && !attr_set[dev]) {
         cudaError_t e = cudaFuncSetAttribute(k_cluster<FMT, TEAM, NITER>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)cluster_smem_bytes(TEAM, 1024));
+                                             (int)cluster_smem_bytes(TEAM, 256));
         if (e != cudaSuccess) return e;
         attr_set[dev] = true;
     }

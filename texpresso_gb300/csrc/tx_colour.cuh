@@ -26,8 +26,9 @@ namespace tx {
 static __constant__ uint32_t c_lut[4][256][2];
 
 // ClusterFit candidate lists.  Entry bits: 0-3 i (offset of S(0,i)),
-// 4-11 offset of S(i,j), 12-19 offset of S(j,k) (compress4 only),
-// 20-29 rank of (i,j[,k]) in the reference's loop order at 16 colours.
+// 4-12 offset of S(i,j), 13-21 offset of S(j,k) (compress4 only),
+// 22-31 rank of (i,j[,k]) in the reference's loop order at 16 colours, so
+// comparing entries compares loop positions.
 // Entries are sorted so that the first N[n] are exactly the candidates of an
 // n-colour set (those with max(i+1, j, k) <= n).
 constexpr int kCand4 = 967, kCand3 = 151;
@@ -35,10 +36,11 @@ static __device__ uint32_t g_cand[kCand4 + 1 + kCand3 + 1];
 static __constant__ uint32_t c_ncand4[17];
 static __constant__ uint32_t c_ncand3[17];
 
-// Row offsets of the packed triangular partial-sum table S(a,b), a <= b <= 16.
-__host__ __device__ constexpr int tri_off(int a) { return 17 * a - (a * (a - 1)) / 2; }
-__host__ __device__ constexpr int tri_idx(int a, int b) { return tri_off(a) + (b - a); }
-constexpr int kTri = 153;
+// Partial-sum table S(a,b), 0 <= a <= b <= 16, stored square with a row
+// stride of 17 float4: the entries that lanes load together (consecutive b,
+// or column b = 16 across rows) fall into different shared-memory banks.
+__host__ __device__ constexpr int sq_idx(int a, int b) { return 17 * a + b; }
+constexpr int kSq = 17 * 17;
 
 // ===========================================================================
 // Shared pieces
@@ -137,10 +139,20 @@ __device__ __forceinline__ uint32_t u8_of(uint32_t px, int c) { return (px >> (8
 // ===========================================================================
 // k_range: one thread per block
 
+// Per-thread point store for the thread-per-block path: pixel i of thread t
+// lives at pts[i * stride + t] as (x, y, z, weight), so a warp's loads of one
+// pixel are 512 contiguous bytes (no bank conflicts) and the fit keeps only
+// accumulators in registers.
+struct PointCol {
+    float4 *base;
+    int stride;
+    __device__ __forceinline__ float4 &operator[](int i) const { return base[i * stride]; }
+};
+
 template <int FMT>
 __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], uint32_t inb,
                                                      const DevParams &prm, const float *s_unorm,
-                                                     const float *s_sqrt) {
+                                                     const float *s_sqrt, const PointCol &pt) {
     // ColourSet (colourset.rs:35-112), pixel-indexed: a "point" is the first
     // pixel of its colour, and pixel order is point order.
     uint32_t tbits = 0;
@@ -151,21 +163,23 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
     }
     const uint32_t valid = inb & ~tbits;
     const bool transparent = tbits != 0;
-    uint32_t key[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) key[i] = ((valid >> i) & 1u) ? (px[i] & 0xFFFFFFu) : (0x01000000u | (uint32_t)i);
-    int rep[16];
     uint32_t newbits = 0;
-    uint64_t dupc = 0;
+    uint64_t repn = 0;  // nibble p: pixel index of p's first occurrence
+    uint64_t dupc = 0;  // nibble p: further pixels sharing p's colour
+    {
+        uint32_t key[16];
 #pragma unroll
-    for (int i = 0; i < 16; ++i) {
-        int r = i;
+        for (int i = 0; i < 16; ++i) key[i] = ((valid >> i) & 1u) ? (px[i] & 0xFFFFFFu) : (0x01000000u | (uint32_t)i);
 #pragma unroll
-        for (int j = i - 1; j >= 0; --j) r = (key[j] == key[i]) ? j : r;
-        rep[i] = r;
-        if ((valid >> i) & 1u) {
-            if (r == i) newbits |= 1u << i;
-            else dupc += 1ull << (4 * r);
+        for (int i = 0; i < 16; ++i) {
+            int r = i;
+#pragma unroll
+            for (int j = i - 1; j >= 0; --j) r = (key[j] == key[i]) ? j : r;
+            repn |= (uint64_t)r << (4 * i);
+            if ((valid >> i) & 1u) {
+                if (r == i) newbits |= 1u << i;
+                else dupc += 1ull << (4 * r);
+            }
         }
     }
     const int count = __popc(newbits);
@@ -179,64 +193,71 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
         for (int c = 0; c < 3; ++c) col[c] = f32_to_i32_clamped(s_unorm[u8_of(rgb, c)] * 255.0f, 255);
         return single_fit<FMT>(col, valid, transparent);
     }
-    float x[16], y[16], z[16], w[16];
-#pragma unroll
-    for (int i = 0; i < 16; ++i) {
-        x[i] = s_unorm[u8_of(px[i], 0)];
-        y[i] = s_unorm[u8_of(px[i], 1)];
-        z[i] = s_unorm[u8_of(px[i], 2)];
-    }
+
+    // Points and weights.  Pixels that are not points get weight exactly 0,
+    // which makes their terms +-0 in every ordered sum below.  Those sums start
+    // at +0 and add non-negative values (total, centroid) or can only reach
+    // zero as +0 (round-to-nearest x + (-x) = +0), so they are never -0 and
+    // adding +-0 leaves them unchanged: the sums equal the reference's sums
+    // over points.
     if (!prm.alpha_weighted) {
 #pragma unroll
-        for (int i = 0; i < 16; ++i) w[i] = s_sqrt[1 + (int)((dupc >> (4 * i)) & 0xFu)];
+        for (int i = 0; i < 16; ++i) {
+            const float w = ((newbits >> i) & 1u) ? s_sqrt[1 + (int)((dupc >> (4 * i)) & 0xFu)] : 0.0f;
+            pt[i] = make_float4(s_unorm[u8_of(px[i], 0)], s_unorm[u8_of(px[i], 1)], s_unorm[u8_of(px[i], 2)], w);
+        }
     } else {
-        float wa[16];
-#pragma unroll
-        for (int i = 0; i < 16; ++i) wa[i] = (float)((px[i] >> 24) + 1u) * (1.0f / 256.0f);
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
             float acc = 0.0f;
 #pragma unroll
-            for (int i = j; i < 16; ++i) acc = acc + ((((valid >> i) & 1u) && rep[i] == j) ? wa[i] : 0.0f);
-            w[j] = sqrt_rn(acc);
+            for (int i = j; i < 16; ++i) {
+                const float wa = (float)((px[i] >> 24) + 1u) * (1.0f / 256.0f);
+                acc = acc + ((((valid >> i) & 1u) && (int)((repn >> (4 * i)) & 0xFu) == j) ? wa : 0.0f);
+            }
+            const float w = ((newbits >> j) & 1u) ? sqrt_rn(acc) : 0.0f;
+            pt[j] = make_float4(s_unorm[u8_of(px[j], 0)], s_unorm[u8_of(px[j], 1)], s_unorm[u8_of(px[j], 2)], w);
         }
     }
 
     // Sym3x3::weighted_covariance (math.rs:44-73)
     float total = 0.0f, cx = 0.0f, cy = 0.0f, cz = 0.0f;
-#pragma unroll
-    for (int i = 0; i < 16; ++i)
-        if ((newbits >> i) & 1u) total = total + w[i];
-#pragma unroll
-    for (int i = 0; i < 16; ++i)
-        if ((newbits >> i) & 1u) { cx = cx + x[i] * w[i]; cy = cy + y[i] * w[i]; cz = cz + z[i] * w[i]; }
+#pragma unroll 4
+    for (int i = 0; i < 16; ++i) {
+        const float4 q = pt[i];
+        total = total + q.w;
+        cx = cx + q.x * q.w; cy = cy + q.y * q.w; cz = cz + q.z * q.w;
+    }
     if (total > FLT_EPSILON) { cx = div_rn(cx, total); cy = div_rn(cy, total); cz = div_rn(cz, total); }
     float m[6] = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
-#pragma unroll
+#pragma unroll 4
     for (int i = 0; i < 16; ++i) {
-        if ((newbits >> i) & 1u) {
-            const float ax = x[i] - cx, ay = y[i] - cy, az = z[i] - cz;
-            const float bx = ax * w[i], by = ay * w[i], bz = az * w[i];
-            m[0] += ax * bx; m[1] += ax * by; m[2] += ax * bz;
-            m[3] += ay * by; m[4] += ay * bz; m[5] += az * bz;
-        }
+        const float4 q = pt[i];
+        const float ax = q.x - cx, ay = q.y - cy, az = q.z - cz;
+        const float bx = ax * q.w, by = ay * q.w, bz = az * q.w;
+        m[0] += ax * bx; m[1] += ax * by; m[2] += ax * bz;
+        m[3] += ay * by; m[4] += ay * bz; m[5] += az * bz;
     }
     float axis[3];
     principle_component(m, axis);
 
-    // RangeFit::new (range.rs:44-101)
+    // RangeFit::new (range.rs:44-101): the first point starts both ends; a later
+    // point moves start on a strictly smaller dot, else end on a strictly larger one
     float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, e0 = 0.0f, e1 = 0.0f, e2 = 0.0f;
     {
         bool seen = false;
         float mn = 0.0f, mx = 0.0f;
-#pragma unroll
+#pragma unroll 4
         for (int i = 0; i < 16; ++i) {
-            if ((newbits >> i) & 1u) {
-                const float d = x[i] * axis[0] + y[i] * axis[1] + z[i] * axis[2];
-                if (!seen) { s0 = e0 = x[i]; s1 = e1 = y[i]; s2 = e2 = z[i]; mn = mx = d; seen = true; }
-                else if (d < mn) { s0 = x[i]; s1 = y[i]; s2 = z[i]; mn = d; }
-                else if (d > mx) { e0 = x[i]; e1 = y[i]; e2 = z[i]; mx = d; }
-            }
+            const float4 q = pt[i];
+            const bool p = (newbits >> i) & 1u;
+            const float d = q.x * axis[0] + q.y * axis[1] + q.z * axis[2];
+            const bool first = p && !seen;
+            const bool lo = first || (p && d < mn);
+            const bool hi = first || (p && !(d < mn) && d > mx);
+            s0 = lo ? q.x : s0; s1 = lo ? q.y : s1; s2 = lo ? q.z : s2; mn = lo ? d : mn;
+            e0 = hi ? q.x : e0; e1 = hi ? q.y : e1; e2 = hi ? q.z : e2; mx = hi ? d : mx;
+            seen = seen || p;
         }
     }
     s0 = snap(s0, 31.0f, 1.0f / 31.0f); s1 = snap(s1, 63.0f, 1.0f / 63.0f); s2 = snap(s2, 31.0f, 1.0f / 31.0f);
@@ -246,33 +267,36 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
     float best_err = FLT_MAX;
     uint2 best = make_uint2(0u, 0u);
 
-    // compression_helper (range.rs:103-143) over a codebook of NC codes
+    // compression_helper (range.rs:103-143) over a codebook of nc codes.  The
+    // error sum adds +0 for pixels that are not points (it starts at +0 and
+    // its terms are non-negative).
     auto helper = [&](const float (&cr)[4], const float (&cg)[4], const float (&cb)[4], int nc,
                       uint32_t &indices) -> bool {
         uint32_t closest = 0;
         float err = 0.0f;
-#pragma unroll
+#pragma unroll 4
         for (int i = 0; i < 16; ++i) {
-            if ((newbits >> i) & 1u) {
-                float dist = FLT_MAX;
-                uint32_t idx = 0;
+            const float4 q = pt[i];
+            float dist = FLT_MAX;
+            uint32_t idx = 0;
 #pragma unroll
-                for (int j = 0; j < 4; ++j) {
-                    if (j < nc) {
-                        const float dx = w0 * (x[i] - cr[j]), dy = w1 * (y[i] - cg[j]), dz = w2 * (z[i] - cb[j]);
-                        const float d = dx * dx + dy * dy + dz * dz;
-                        if (d < dist) { dist = d; idx = (uint32_t)j; }
-                    }
+            for (int j = 0; j < 4; ++j) {
+                if (j < nc) {
+                    const float dx = w0 * (q.x - cr[j]), dy = w1 * (q.y - cg[j]), dz = w2 * (q.z - cb[j]);
+                    const float d = dx * dx + dy * dy + dz * dz;
+                    idx = d < dist ? (uint32_t)j : idx;
+                    dist = d < dist ? d : dist;
                 }
-                closest |= idx << (2 * i);
-                err += dist;
             }
+            closest |= idx << (2 * i);
+            err = err + (((newbits >> i) & 1u) ? dist : 0.0f);
         }
         if (err < best_err) {
             uint32_t out = 0;
 #pragma unroll
             for (int p = 0; p < 16; ++p) {
-                const uint32_t v = ((valid >> p) & 1u) ? ((closest >> (2 * rep[p])) & 3u) : 3u;
+                const uint32_t r = (uint32_t)((repn >> (4 * p)) & 0xFu);
+                const uint32_t v = ((valid >> p) & 1u) ? ((closest >> (2 * r)) & 3u) : 3u;
                 out |= v << (2 * p);
             }
             indices = out;
@@ -336,21 +360,34 @@ struct Team {
 };
 
 struct __align__(16) TeamSmem {
-    float4 S[kTri + 3];     // S(a,b) running sums, packed triangle (+pad)
+    float4 S[kSq + 3];      // S(a,b) running sums, S[17a + b] (+pad)
     float4 PW[16];          // points_weights in the current ordering
     float P[4][16];         // x, y, z, weight of each point, point order
     float D[16];            // dot products
     uint32_t hist[8][4];    // orderings of earlier iterations (16 bytes each)
 };
 
-// fcmp of cluster.rs:90-97 as "a sorts before b" / "a and b tie".
-__device__ __forceinline__ bool dps_less(float a, float b) {
-    const bool fa = isfinite(a), fb = isfinite(b);
-    return fa && (!fb || a < b);
+// Sort key of cluster.rs:90-97 as an unsigned integer: finite values keep
+// their order (-0 and +0 tie), every non-finite value ties after all finite
+// ones.  Comparing keys is comparing with fcmp.
+__device__ __forceinline__ uint32_t dps_key(float x) {
+    if (!isfinite(x)) return 0xFFFFFFFFu;
+    const uint32_t u = (uint32_t)__float_as_int(x + 0.0f);  // -0 -> +0
+    return (u & 0x80000000u) ? ~u : (u | 0x80000000u);
 }
-__device__ __forceinline__ bool dps_equiv(float a, float b) {
-    const bool fa = isfinite(a), fb = isfinite(b);
-    return (!fa && !fb) || (fa && fb && a == b);
+
+// min(1, max(0, fl(a * b))) in one instruction: mul.rn with .sat clamps the
+// rounded product to [0, 1] and turns NaN into +0, as f32::max/min do in
+// cluster.rs:207-208 (max(0, NaN) = 0).
+__device__ __forceinline__ float mul_sat(float a, float b) {
+    float d;
+    asm("mul.rn.sat.f32 %0, %1, %2;" : "=f"(d) : "f"(a), "f"(b));
+    return d;
+}
+
+// Snap a value already clamped to [0, 1] to the grid (cluster.rs:209-210).
+__device__ __forceinline__ float snap01(float x, float grid, float gridrcp) {
+    return truncf(grid * x + 0.5f) * gridrcp;
 }
 
 __device__ __forceinline__ uint8_t hist_get(const TeamSmem &sm, int it, int m) {
@@ -380,12 +417,12 @@ __device__ __forceinline__ float eval4(const float4 p0, const float4 p1, const f
     float e5[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float a = snap(((ax[c] * beta2) - bx[c] * ab) * factor, grid[c], gridrcp[c]);
-        const float b = snap(((bx[c] * alpha2) - ax[c] * ab) * factor, grid[c], gridrcp[c]);
+        const float a = snap01(mul_sat((ax[c] * beta2) - bx[c] * ab, factor), grid[c], gridrcp[c]);
+        const float b = snap01(mul_sat((bx[c] * alpha2) - ax[c] * ab, factor), grid[c], gridrcp[c]);
         const float e1 = (a * a) * alpha2 + (b * b * beta2);
         const float e2 = (a * b * ab) - a * ax[c];
         const float e3 = e2 - b * bx[c];
-        const float e4 = 2.0f * e3 + e1;
+        const float e4 = __fmaf_rn(2.0f, e3, e1);  // 2*e3 is exact, so this equals fl(fl(2*e3) + e1)
         e5[c] = e4 * cw[c];
         if (WANT_AB) { ea[c] = a; eb[c] = b; }
     }
@@ -398,24 +435,24 @@ __device__ __forceinline__ float eval3(const float4 p0, const float4 p1, const f
                                        float (&ea)[3], float (&eb)[3]) {
     const float p2x = xs.x - p1.x - p0.x, p2y = xs.y - p1.y - p0.y, p2z = xs.z - p1.z - p0.z,
                 p2w = xs.w - p1.w - p0.w;
-    const float tx = p1.x * 0.5f, ty = p1.y * 0.5f, tz = p1.z * 0.5f, tw = p1.w * 0.25f;
-    const float ax[3] = {tx + p0.x, ty + p0.y, tz + p0.z};
-    const float alpha2 = tw + p0.w;
-    const float bx[3] = {tx + p2x, ty + p2y, tz + p2z};
-    const float beta2 = tw + p2w;
-    const float ab = tw;
+    // part1 * (0.5, 0.5, 0.5, 0.25) is exact, so each sum is one fused op
+    const float ax[3] = {__fmaf_rn(p1.x, 0.5f, p0.x), __fmaf_rn(p1.y, 0.5f, p0.y), __fmaf_rn(p1.z, 0.5f, p0.z)};
+    const float alpha2 = __fmaf_rn(p1.w, 0.25f, p0.w);
+    const float bx[3] = {__fmaf_rn(p1.x, 0.5f, p2x), __fmaf_rn(p1.y, 0.5f, p2y), __fmaf_rn(p1.z, 0.5f, p2z)};
+    const float beta2 = __fmaf_rn(p1.w, 0.25f, p2w);
+    const float ab = p1.w * 0.25f;
     const float factor = rcp_rn((alpha2 * beta2) - ab * ab);
     const float grid[3] = {31.0f, 63.0f, 31.0f};
     const float gridrcp[3] = {1.0f / 31.0f, 1.0f / 63.0f, 1.0f / 31.0f};
     float e5[3];
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        const float a = snap(((ax[c] * beta2) - bx[c] * ab) * factor, grid[c], gridrcp[c]);
-        const float b = snap(((bx[c] * alpha2) - ax[c] * ab) * factor, grid[c], gridrcp[c]);
+        const float a = snap01(mul_sat((ax[c] * beta2) - bx[c] * ab, factor), grid[c], gridrcp[c]);
+        const float b = snap01(mul_sat((bx[c] * alpha2) - ax[c] * ab, factor), grid[c], gridrcp[c]);
         const float e1 = (a * a) * alpha2 + (b * b * beta2);
         const float e2 = (a * b * ab) - a * ax[c];
         const float e3 = e2 - b * bx[c];
-        const float e4 = 2.0f * e3 + e1;
+        const float e4 = __fmaf_rn(2.0f, e3, e1);
         e5[c] = e4 * cw[c];
         if (WANT_AB) { ea[c] = a; eb[c] = b; }
     }
@@ -425,8 +462,8 @@ __device__ __forceinline__ float eval3(const float4 p0, const float4 p1, const f
 // Decode (i, j, k) from a candidate entry.
 __device__ __forceinline__ void decode_entry(uint32_t e, int &i, int &j, int &k) {
     i = (int)(e & 0xFu);
-    j = (int)((e >> 4) & 0xFFu) - tri_off(i) + i;
-    k = (int)((e >> 12) & 0xFFu) - tri_off(j) + j;
+    j = (int)((e >> 4) & 0x1FFu) - 17 * i;
+    k = (int)((e >> 13) & 0x1FFu) - 17 * j;
 }
 
 // ClusterFit::compress3 / compress4 (cluster.rs:152-417) for one team.
@@ -449,14 +486,16 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
         // construct_ordering (cluster.rs:78-136)
         float de = FLT_MAX;
         if (lane < count) de = sm.P[0][lane] * axis[0] + sm.P[1][lane] * axis[1] + sm.P[2][lane] * axis[2];
-        if (lane < 16) sm.D[lane] = de;
+        const uint32_t ke = dps_key(de);
+        if (lane < 16) reinterpret_cast<uint32_t *>(sm.D)[lane] = ke;
         tm.sync();
         if (lane < 16) {
+            // stable rank: entries with a smaller key, or an equal key earlier
             int rank = 0;
 #pragma unroll
             for (int f = 0; f < 16; ++f) {
-                const float df = sm.D[f];
-                rank += (dps_less(df, de) || (f < lane && dps_equiv(df, de))) ? 1 : 0;
+                const uint32_t kf = reinterpret_cast<const uint32_t *>(sm.D)[f];
+                rank += (kf < ke || (kf == ke && f < lane)) ? 1 : 0;
             }
             reinterpret_cast<uint8_t *>(sm.hist[it])[rank] = (uint8_t)(lane < count ? lane : 0);
         }
@@ -473,11 +512,11 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
         tm.sync();
         // partial sums S(a,b) = pw[a] + ... + pw[b-1], accumulated from zero in
         // loop order exactly like part0/part1/part2 of the reference
-        if (lane == 0) sm.S[tri_idx(count, count)] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (lane == 0) sm.S[sq_idx(count, count)] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (lane < count) {
             float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-            sm.S[tri_idx(lane, lane)] = acc;
-            const int o = tri_off(lane) - lane;
+            sm.S[sq_idx(lane, lane)] = acc;
+            const int o = 17 * lane;
             for (int b = lane; b < count; ++b) {
                 const float4 q = sm.PW[b];
                 acc.x += q.x; acc.y += q.y; acc.z += q.z; acc.w += q.w;
@@ -488,21 +527,23 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
         xs = sm.S[count];  // S(0, count) == xsum_wsum
 
         // the sweep: lane-strided over the candidate list
-        float lbest = __int_as_float(0x7f800000);
-        uint32_t lent = 0xFFFFFFFFu;
+        // (lbest, lent) starts at (run, 0): no entry is below 0, so a candidate
+        // that only ties the running best never wins; NaN never compares true
+        float lbest = run;
+        uint32_t lent = 0;
         float dummy_a[3], dummy_b[3];
         for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
             const uint32_t e = tbl[t];
             const float4 p0 = sm.S[e & 0xFu];
-            const float4 p1 = sm.S[(e >> 4) & 0xFFu];
+            const float4 p1 = sm.S[(e >> 4) & 0x1FFu];
             float err;
             if (NC == 4) {
-                const float4 p2 = sm.S[(e >> 12) & 0xFFu];
+                const float4 p2 = sm.S[(e >> 13) & 0x1FFu];
                 err = eval4<false>(p0, p1, p2, xs, cw, dummy_a, dummy_b);
             } else {
                 err = eval3<false>(p0, p1, xs, cw, dummy_a, dummy_b);
             }
-            if (err < run && (err < lbest || (err == lbest && e < lent))) { lbest = err; lent = e; }
+            if (err < lbest || (err == lbest && e < lent)) { lbest = err; lent = e; }
         }
 #pragma unroll
         for (int off = TEAM / 2; off > 0; off >>= 1) {
@@ -510,14 +551,14 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
             const uint32_t on = tm.shfl_xor(lent, off);
             if (oe < lbest || (oe == lbest && on < lent)) { lbest = oe; lent = on; }
         }
-        if (lent != 0xFFFFFFFFu) {
+        if (lent != 0u) {
             run = lbest;
             bentry = lent;
             bit = it;
             const float4 p0 = sm.S[lent & 0xFu];
-            const float4 p1 = sm.S[(lent >> 4) & 0xFFu];
+            const float4 p1 = sm.S[(lent >> 4) & 0x1FFu];
             if (NC == 4) {
-                const float4 p2 = sm.S[(lent >> 12) & 0xFFu];
+                const float4 p2 = sm.S[(lent >> 13) & 0x1FFu];
                 eval4<true>(p0, p1, p2, xs, cw, ba, bb);
             } else {
                 eval3<true>(p0, p1, xs, cw, ba, bb);
@@ -689,21 +730,20 @@ __device__ __forceinline__ uint2 team_bc3_alpha(const Team<TEAM> &tm, uint32_t v
 // Thread-per-block: encode and store block b (RangeFit / SingleColourFit path).
 template <int FMT>
 __device__ __forceinline__ void range_block(const SrcDesc &src, size_t b, const DevParams &prm, uint8_t *out,
-                                            const float *s_unorm, const float *s_sqrt) {
+                                            const float *s_unorm, const float *s_sqrt, const PointCol &pt) {
     uint32_t px[16];
     const uint32_t mask = load_block_rgba(src, b, px);
-    const uint2 col = colour_range_thread<FMT>(px, mask, prm, s_unorm, s_sqrt);
-    if (FMT == BC1) {
-        reinterpret_cast<uint2 *>(out)[b] = col;
-    } else {
-        uint2 al = (FMT == BC2) ? encode_bc2_alpha(px, mask) : make_uint2(0u, 0u);
-        if (FMT == BC3) {
-            uint32_t v[4];
-            channel_words(px, 3, v);
-            al = encode_bc3_alpha(v, mask);
-        }
-        reinterpret_cast<uint4 *>(out)[b] = make_uint4(al.x, al.y, col.x, col.y);
+    // alpha first, so the alpha bytes are dead before the colour fit's registers peak
+    uint2 al = make_uint2(0u, 0u);
+    if (FMT == BC2) al = encode_bc2_alpha(px, mask);
+    if (FMT == BC3) {
+        uint32_t v[4];
+        channel_words(px, 3, v);
+        al = encode_bc3_alpha(v, mask);
     }
+    const uint2 col = colour_range_thread<FMT>(px, mask, prm, s_unorm, s_sqrt, pt);
+    if (FMT == BC1) reinterpret_cast<uint2 *>(out)[b] = col;
+    else reinterpret_cast<uint4 *>(out)[b] = make_uint4(al.x, al.y, col.x, col.y);
 }
 
 // Team-per-block: encode and store block b (ClusterFit path).
@@ -765,8 +805,8 @@ static inline cudaError_t upload_tables_this_tu(const uint32_t lut[4][256][2]) {
                 const int m = (i + 1 > j ? i + 1 : j) > k ? (i + 1 > j ? i + 1 : j) : k;
                 c4[n4].m = m;
                 c4[n4].rank = n4;
-                c4[n4].e = (uint32_t)i | ((uint32_t)tri_idx(i, j) << 4) | ((uint32_t)tri_idx(j, k) << 12) |
-                           ((uint32_t)n4 << 20);
+                c4[n4].e = (uint32_t)i | ((uint32_t)sq_idx(i, j) << 4) | ((uint32_t)sq_idx(j, k) << 13) |
+                           ((uint32_t)n4 << 22);
                 ++n4;
             }
     for (int i = 0; i < 16; ++i)
@@ -774,7 +814,7 @@ static inline cudaError_t upload_tables_this_tu(const uint32_t lut[4][256][2]) {
             const int m = i + 1 > j ? i + 1 : j;
             c3[n3].m = m;
             c3[n3].rank = n3;
-            c3[n3].e = (uint32_t)i | ((uint32_t)tri_idx(i, j) << 4) | ((uint32_t)n3 << 20);
+            c3[n3].e = (uint32_t)i | ((uint32_t)sq_idx(i, j) << 4) | ((uint32_t)n3 << 22);
             ++n3;
         }
     if (n4 != kCand4 || n3 != kCand3) return cudaErrorInvalidValue;
