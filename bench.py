@@ -258,26 +258,22 @@ def e2e_time(torch, tx, fmt, img, params, steps, warmup):
 # CPU (oracle) timing
 
 def cpu_rate(oracle, fmt, img, params, seconds, nthreads=0):
-    """Mblocks/s of the oracle over repeated passes (or bands) for ~seconds."""
+    """Mblocks/s of the oracle over whole passes of img for at least `seconds`
+    (one pass at least; a pass larger than the budget is cut to a band of rows)."""
     h, w = img.shape[:2]
     bw = (w + 3) // 4
     rows_total = (h + 3) // 4
-    # calibrate on a band of 1/16 of the rows
     band = max(1, rows_total // 16)
     t0 = time.perf_counter()
-    oracle.compress(fmt, img[:4 * band], w, 4 * band, params, nthreads=nthreads)
+    oracle.compress(fmt, img[:4 * band], w, min(h, 4 * band), params, nthreads=nthreads)
     per_row = (time.perf_counter() - t0) / band
     rows = int(min(rows_total, max(1, seconds / max(per_row, 1e-9))))
     blocks = 0
     t0 = time.perf_counter()
     while True:
-        r0 = 0
-        while r0 < rows_total and blocks < rows * bw:
-            r1 = min(rows_total, r0 + rows)
-            oracle.compress(fmt, img[4 * r0:4 * r1], w, min(h, 4 * r1) - 4 * r0, params, nthreads=nthreads)
-            blocks += (r1 - r0) * bw
-            r0 = r1
-        if time.perf_counter() - t0 >= seconds or blocks >= rows * bw:
+        oracle.compress(fmt, img[:4 * rows], w, min(h, 4 * rows), params, nthreads=nthreads)
+        blocks += rows * bw
+        if time.perf_counter() - t0 >= seconds:
             break
     dt = time.perf_counter() - t0
     return blocks / dt / 1e6, blocks, dt

@@ -3,6 +3,8 @@
 #include "tx_colour.cuh"
 #include "tx_internal.h"
 
+#include <cstdlib>
+
 namespace tx {
 
 template <int FMT>
@@ -77,10 +79,21 @@ static cudaError_t launch_cluster_t(const SrcDesc &src, const DevParams &prm, ui
     return cudaGetLastError();
 }
 
+// Lanes per block of the single-texture ClusterFit kernel: 32 unless the
+// TX_CLUSTER_TEAM environment variable asks for 16 (read once).
+static int cluster_team_override() {
+    static const int v = [] {
+        const char *e = getenv("TX_CLUSTER_TEAM");
+        return (e && atoi(e) == 16) ? 16 : (e && atoi(e) == 32) ? 32 : 0;
+    }();
+    return v;
+}
+
 template <int FMT, int NITER>
 static cudaError_t launch_cluster_team(const SrcDesc &src, const DevParams &prm, uint8_t *out, size_t nblocks,
                                        cudaStream_t st, const LaunchCfg &cfg) {
-    if (cfg.cluster_team == 16) return launch_cluster_t<FMT, 16, NITER>(src, prm, out, nblocks, st, cfg);
+    const int team = cluster_team_override() ? cluster_team_override() : cfg.cluster_team;
+    if (team == 16) return launch_cluster_t<FMT, 16, NITER>(src, prm, out, nblocks, st, cfg);
     return launch_cluster_t<FMT, 32, NITER>(src, prm, out, nblocks, st, cfg);
 }
 

@@ -35,6 +35,13 @@ constexpr int kCand4 = 967, kCand3 = 151;
 static __device__ uint32_t g_cand[kCand4 + 1 + kCand3 + 1];
 static __constant__ uint32_t c_ncand4[17];
 static __constant__ uint32_t c_ncand3[17];
+// Weight-lane terms (alpha2, beta2, alphabeta, factor) of every candidate of a
+// 16-colour set whose point weights are all exactly 1: the partial sums' w
+// lanes are then the counts i, j-i, k-j, so the terms depend on the candidate
+// alone.  Filled on the device by k_unit_terms with the same f32 code the
+// sweep would run (wterms4 / wterms3), so loading them is exact.
+static __device__ float4 g_unit4[kCand4 + 1];
+static __device__ float4 g_unit3[kCand3 + 1];
 
 // Partial-sum table S(a,b), 0 <= a <= b <= 16, stored square with a row
 // stride of 17 float4: the entries that lanes load together (consecutive b,
@@ -394,24 +401,32 @@ __device__ __forceinline__ uint8_t hist_get(const TeamSmem &sm, int it, int m) {
     return reinterpret_cast<const uint8_t *>(sm.hist[it])[m];
 }
 
-// One compress4 candidate (cluster.rs:320-353).  Returns the error, writes
-// the snapped endpoints when WANT_AB.
+// Weight-lane terms of one compress4 candidate (cluster.rs:320-335).
+__device__ __forceinline__ float4 wterms4(float p0w, float p1w, float p2w, float xsw) {
+    const float c19 = 1.0f / 9.0f, c49 = 4.0f / 9.0f, c29 = 2.0f / 9.0f;
+    const float p3w = xsw - p2w - p1w - p0w;
+    const float alpha2 = p2w * c19 + (p1w * c49 + p0w);
+    const float beta2 = p1w * c19 + (p2w * c49 + p3w);
+    const float ab = c29 * (p1w + p2w);
+    return make_float4(alpha2, beta2, ab, rcp_rn((alpha2 * beta2) - ab * ab));
+}
+
+// Weight-lane terms of one compress3 candidate (cluster.rs:189-202).  The
+// products part1 * (.5, .25) are exact, so each sum is one fused op.
+__device__ __forceinline__ float4 wterms3(float p0w, float p1w, float xsw) {
+    const float p2w = xsw - p1w - p0w;
+    const float alpha2 = __fmaf_rn(p1w, 0.25f, p0w);
+    const float beta2 = __fmaf_rn(p1w, 0.25f, p2w);
+    const float ab = p1w * 0.25f;
+    return make_float4(alpha2, beta2, ab, rcp_rn((alpha2 * beta2) - ab * ab));
+}
+
+// Endpoint fit and error of one candidate given its x/y/z sums ax, bx and its
+// weight-lane terms wt (cluster.rs:200-220, :333-353).
 template <bool WANT_AB>
-__device__ __forceinline__ float eval4(const float4 p0, const float4 p1, const float4 p2, const float4 xs,
-                                       const float (&cw)[3], float (&ea)[3], float (&eb)[3]) {
-    const float c13 = 1.0f / 3.0f, c19 = 1.0f / 9.0f, c23 = 2.0f / 3.0f, c49 = 4.0f / 9.0f, c29 = 2.0f / 9.0f;
-    const float p3x = xs.x - p2.x - p1.x - p0.x;
-    const float p3y = xs.y - p2.y - p1.y - p0.y;
-    const float p3z = xs.z - p2.z - p1.z - p0.z;
-    const float p3w = xs.w - p2.w - p1.w - p0.w;
-    const float ax[3] = {p2.x * c13 + (p1.x * c23 + p0.x), p2.y * c13 + (p1.y * c23 + p0.y),
-                         p2.z * c13 + (p1.z * c23 + p0.z)};
-    const float alpha2 = p2.w * c19 + (p1.w * c49 + p0.w);
-    const float bx[3] = {p1.x * c13 + (p2.x * c23 + p3x), p1.y * c13 + (p2.y * c23 + p3y),
-                         p1.z * c13 + (p2.z * c23 + p3z)};
-    const float beta2 = p1.w * c19 + (p2.w * c49 + p3w);
-    const float ab = c29 * (p1.w + p2.w);
-    const float factor = rcp_rn((alpha2 * beta2) - ab * ab);
+__device__ __forceinline__ float fit_error(const float (&ax)[3], const float (&bx)[3], const float4 wt,
+                                           const float (&cw)[3], float (&ea)[3], float (&eb)[3]) {
+    const float alpha2 = wt.x, beta2 = wt.y, ab = wt.z, factor = wt.w;
     const float grid[3] = {31.0f, 63.0f, 31.0f};
     const float gridrcp[3] = {1.0f / 31.0f, 1.0f / 63.0f, 1.0f / 31.0f};
     float e5[3];
@@ -429,34 +444,29 @@ __device__ __forceinline__ float eval4(const float4 p0, const float4 p1, const f
     return e5[0] + e5[1] + e5[2];
 }
 
-// One compress3 candidate (cluster.rs:189-220).
+// One compress4 candidate (cluster.rs:320-353); wt = wterms4(...) of its w lanes.
 template <bool WANT_AB>
-__device__ __forceinline__ float eval3(const float4 p0, const float4 p1, const float4 xs, const float (&cw)[3],
-                                       float (&ea)[3], float (&eb)[3]) {
-    const float p2x = xs.x - p1.x - p0.x, p2y = xs.y - p1.y - p0.y, p2z = xs.z - p1.z - p0.z,
-                p2w = xs.w - p1.w - p0.w;
-    // part1 * (0.5, 0.5, 0.5, 0.25) is exact, so each sum is one fused op
+__device__ __forceinline__ float eval4(const float4 p0, const float4 p1, const float4 p2, const float4 xs,
+                                       const float4 wt, const float (&cw)[3], float (&ea)[3], float (&eb)[3]) {
+    const float c13 = 1.0f / 3.0f, c23 = 2.0f / 3.0f;
+    const float p3x = xs.x - p2.x - p1.x - p0.x;
+    const float p3y = xs.y - p2.y - p1.y - p0.y;
+    const float p3z = xs.z - p2.z - p1.z - p0.z;
+    const float ax[3] = {p2.x * c13 + (p1.x * c23 + p0.x), p2.y * c13 + (p1.y * c23 + p0.y),
+                         p2.z * c13 + (p1.z * c23 + p0.z)};
+    const float bx[3] = {p1.x * c13 + (p2.x * c23 + p3x), p1.y * c13 + (p2.y * c23 + p3y),
+                         p1.z * c13 + (p2.z * c23 + p3z)};
+    return fit_error<WANT_AB>(ax, bx, wt, cw, ea, eb);
+}
+
+// One compress3 candidate (cluster.rs:189-220); wt = wterms3(...) of its w lanes.
+template <bool WANT_AB>
+__device__ __forceinline__ float eval3(const float4 p0, const float4 p1, const float4 xs, const float4 wt,
+                                       const float (&cw)[3], float (&ea)[3], float (&eb)[3]) {
+    const float p2x = xs.x - p1.x - p0.x, p2y = xs.y - p1.y - p0.y, p2z = xs.z - p1.z - p0.z;
     const float ax[3] = {__fmaf_rn(p1.x, 0.5f, p0.x), __fmaf_rn(p1.y, 0.5f, p0.y), __fmaf_rn(p1.z, 0.5f, p0.z)};
-    const float alpha2 = __fmaf_rn(p1.w, 0.25f, p0.w);
     const float bx[3] = {__fmaf_rn(p1.x, 0.5f, p2x), __fmaf_rn(p1.y, 0.5f, p2y), __fmaf_rn(p1.z, 0.5f, p2z)};
-    const float beta2 = __fmaf_rn(p1.w, 0.25f, p2w);
-    const float ab = p1.w * 0.25f;
-    const float factor = rcp_rn((alpha2 * beta2) - ab * ab);
-    const float grid[3] = {31.0f, 63.0f, 31.0f};
-    const float gridrcp[3] = {1.0f / 31.0f, 1.0f / 63.0f, 1.0f / 31.0f};
-    float e5[3];
-#pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const float a = snap01(mul_sat((ax[c] * beta2) - bx[c] * ab, factor), grid[c], gridrcp[c]);
-        const float b = snap01(mul_sat((bx[c] * alpha2) - ax[c] * ab, factor), grid[c], gridrcp[c]);
-        const float e1 = (a * a) * alpha2 + (b * b * beta2);
-        const float e2 = (a * b * ab) - a * ax[c];
-        const float e3 = e2 - b * bx[c];
-        const float e4 = __fmaf_rn(2.0f, e3, e1);
-        e5[c] = e4 * cw[c];
-        if (WANT_AB) { ea[c] = a; eb[c] = b; }
-    }
-    return e5[0] + e5[1] + e5[2];
+    return fit_error<WANT_AB>(ax, bx, wt, cw, ea, eb);
 }
 
 // Decode (i, j, k) from a candidate entry.
@@ -471,7 +481,7 @@ __device__ __forceinline__ void decode_entry(uint32_t e, int &i, int &j, int &k)
 template <int NC, int TEAM, int NITER>
 __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm, const uint32_t *tbl, int count,
                                              const float (&principal)[3], const float (&cw)[3], bool valid,
-                                             int my_point, float &best_err, uint2 &best) {
+                                             int my_point, bool unit16, float &best_err, uint2 &best) {
     const int lane = tm.lane;
     float run = best_err;
     float ba[3] = {0.0f, 0.0f, 0.0f}, bb[3] = {0.0f, 0.0f, 0.0f};
@@ -532,18 +542,33 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
         float lbest = run;
         uint32_t lent = 0;
         float dummy_a[3], dummy_b[3];
-        for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
-            const uint32_t e = tbl[t];
-            const float4 p0 = sm.S[e & 0xFu];
-            const float4 p1 = sm.S[(e >> 4) & 0x1FFu];
-            float err;
-            if (NC == 4) {
-                const float4 p2 = sm.S[(e >> 13) & 0x1FFu];
-                err = eval4<false>(p0, p1, p2, xs, cw, dummy_a, dummy_b);
-            } else {
-                err = eval3<false>(p0, p1, xs, cw, dummy_a, dummy_b);
+        if (unit16) {
+            // 16 points of weight 1: the weight-lane terms come from the table
+            const float4 *ut = NC == 4 ? g_unit4 : g_unit3;
+            for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
+                const uint32_t e = tbl[t];
+                const float4 wt = __ldg(ut + t);
+                const float4 p0 = sm.S[e & 0xFu];
+                const float4 p1 = sm.S[(e >> 4) & 0x1FFu];
+                float err;
+                if (NC == 4) err = eval4<false>(p0, p1, sm.S[(e >> 13) & 0x1FFu], xs, wt, cw, dummy_a, dummy_b);
+                else err = eval3<false>(p0, p1, xs, wt, cw, dummy_a, dummy_b);
+                if (err < lbest || (err == lbest && e < lent)) { lbest = err; lent = e; }
             }
-            if (err < lbest || (err == lbest && e < lent)) { lbest = err; lent = e; }
+        } else {
+            for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
+                const uint32_t e = tbl[t];
+                const float4 p0 = sm.S[e & 0xFu];
+                const float4 p1 = sm.S[(e >> 4) & 0x1FFu];
+                float err;
+                if (NC == 4) {
+                    const float4 p2 = sm.S[(e >> 13) & 0x1FFu];
+                    err = eval4<false>(p0, p1, p2, xs, wterms4(p0.w, p1.w, p2.w, xs.w), cw, dummy_a, dummy_b);
+                } else {
+                    err = eval3<false>(p0, p1, xs, wterms3(p0.w, p1.w, xs.w), cw, dummy_a, dummy_b);
+                }
+                if (err < lbest || (err == lbest && e < lent)) { lbest = err; lent = e; }
+            }
         }
 #pragma unroll
         for (int off = TEAM / 2; off > 0; off >>= 1) {
@@ -559,9 +584,9 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
             const float4 p1 = sm.S[(lent >> 4) & 0x1FFu];
             if (NC == 4) {
                 const float4 p2 = sm.S[(lent >> 13) & 0x1FFu];
-                eval4<true>(p0, p1, p2, xs, cw, ba, bb);
+                eval4<true>(p0, p1, p2, xs, wterms4(p0.w, p1.w, p2.w, xs.w), cw, ba, bb);
             } else {
-                eval3<true>(p0, p1, xs, cw, ba, bb);
+                eval3<true>(p0, p1, xs, wterms3(p0.w, p1.w, xs.w), cw, ba, bb);
             }
         }
         if (bit != it) break;
@@ -668,12 +693,14 @@ __device__ __forceinline__ uint2 colour_cluster_team(const Team<TEAM> &tm, TeamS
     const float cw[3] = {prm.w[0], prm.w[1], prm.w[2]};
     float best_err = FLT_MAX;
     uint2 best = make_uint2(0u, 0u);
+    // 16 distinct colours without alpha weighting: every weight is sqrt(1) = 1
+    const bool unit16 = count == 16 && !prm.alpha_weighted;
     if (FMT == BC1) {
-        cluster_pass<3, TEAM, NITER>(tm, sm, tbl3, count, principal, cw, valid, my_point, best_err, best);
+        cluster_pass<3, TEAM, NITER>(tm, sm, tbl3, count, principal, cw, valid, my_point, unit16, best_err, best);
         if (!transparent)
-            cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, valid, my_point, best_err, best);
+            cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, valid, my_point, unit16, best_err, best);
     } else {
-        cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, valid, my_point, best_err, best);
+        cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, valid, my_point, unit16, best_err, best);
     }
     return best;
 }
@@ -789,6 +816,22 @@ __device__ __forceinline__ void load_cand_tables(uint32_t *tbl) {
     for (int i = threadIdx.x; i < kCandTbl; i += blockDim.x) tbl[i] = g_cand[i];
 }
 
+// Fill g_unit4 / g_unit3 from this TU's candidate lists: the w-lane sums of
+// a 16-point, weight-1 set are S(a,b).w = b - a (exact small integers).
+static __global__ void k_unit_terms() {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t < kCand4) {
+        int i, j, k;
+        decode_entry(g_cand[t], i, j, k);
+        g_unit4[t] = wterms4((float)i, (float)(j - i), (float)(k - j), 16.0f);
+    }
+    if (t < kCand3) {
+        int i, j, k;
+        decode_entry(g_cand[kCand4 + 1 + t], i, j, k);
+        g_unit3[t] = wterms3((float)i, (float)(j - i), 16.0f);
+    }
+}
+
 // ===========================================================================
 // host side: candidate lists + upload of this TU's tables
 
@@ -840,6 +883,9 @@ static inline cudaError_t upload_tables_this_tu(const uint32_t lut[4][256][2]) {
     if ((e = cudaMemcpyToSymbol(g_cand, tbl, sizeof(tbl))) != cudaSuccess) return e;
     if ((e = cudaMemcpyToSymbol(c_ncand4, nc4, sizeof(nc4))) != cudaSuccess) return e;
     if ((e = cudaMemcpyToSymbol(c_ncand3, nc3, sizeof(nc3))) != cudaSuccess) return e;
+    k_unit_terms<<<(kCand4 + 255) / 256, 256>>>();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
     return cudaMemcpyToSymbol(c_lut, lut, sizeof(uint32_t) * 4 * 256 * 2);
 }
 
