@@ -278,6 +278,25 @@ TX_API int tx_server_get_stats(tx_server *server, tx_server_stats *stats);
 /* Finish every queued job, then stop the worker and free the arena. */
 TX_API void tx_server_destroy(tx_server *server);
 
+/* ---------------------------------------------------------------------------
+ * DDS container (host only; cli/src/main.rs:143-196 writes and reads DDS
+ * through the ddsfile crate).  A DDS file is TX_DDS_HEADER_BYTES of header
+ * followed by the compressed levels, level 0 first. */
+#define TX_DDS_HEADER_BYTES 148
+
+/* Write the magic, DDS_HEADER and DDS_HEADER_DXT10 the CLI writes
+ * (cli/src/main.rs:143-164): DXGI BC1/BC2/BC3 UNORM_SRGB, BC4/BC5 UNORM,
+ * Texture2D, alpha mode premultiplied for BC1 and straight otherwise.
+ * mip_levels <= 1 writes no mip count (the CLI's case). */
+TX_API int tx_dds_write_header(int format, uint32_t width, uint32_t height, uint32_t mip_levels,
+                               uint8_t *out, size_t out_len, size_t *written);
+
+/* Read a DDS header as cli/src/main.rs:167-196 does: a DX10 header with the
+ * DXGI formats above and Texture2D, or a legacy DXT1/DXT3/DXT5 FourCC.
+ * Returns TX_ERR_INVALID_FORMAT where the CLI panics on the format. */
+TX_API int tx_dds_parse(const uint8_t *data, size_t len, int *format, uint32_t *width, uint32_t *height,
+                        uint32_t *mip_levels, size_t *data_offset);
+
 /* The CUDA error behind the last TX_ERR_CUDA returned on this thread
  * (a cudaError_t value), or 0. */
 TX_API int tx_last_cuda_error(void);

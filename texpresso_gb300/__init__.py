@@ -427,3 +427,46 @@ class Server:
             self.close()
         except Exception:
             pass
+
+
+# ---------------------------------------------------------------------------
+# DDS container (tx_dds_*)
+
+DDS_HEADER_BYTES = 148
+_lib.tx_dds_write_header.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _sz,
+                                     ctypes.POINTER(_sz)]
+_lib.tx_dds_parse.argtypes = [_vp, _sz, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint32),
+                              ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(_sz)]
+
+
+def dds_header(fmt, width, height, mip_levels=0):
+    """The 148 header bytes the reference CLI writes (cli/src/main.rs:143-164)."""
+    out = bytearray(DDS_HEADER_BYTES)
+    dst, dlen = _buffer(out, True)
+    n = _sz()
+    _check(_lib.tx_dds_write_header(int(fmt), width, height, mip_levels, dst, dlen, ctypes.byref(n)), "dds_header")
+    return bytes(out[:n.value])
+
+
+def dds_parse(data):
+    """(format, width, height, mip_levels, data_offset) of a DDS file's header."""
+    src, slen = _buffer(data, False)
+    f, w, h, m, off = ctypes.c_int(), ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32(), _sz()
+    _check(_lib.tx_dds_parse(src, slen, ctypes.byref(f), ctypes.byref(w), ctypes.byref(h), ctypes.byref(m),
+                             ctypes.byref(off)), "dds_parse")
+    return Format(f.value), w.value, h.value, m.value, off.value
+
+
+def write_dds(path, fmt, width, height, blocks, mip_levels=0):
+    """Write compressed levels as a DDS file, as the reference CLI does."""
+    with open(path, "wb") as f:
+        f.write(dds_header(fmt, width, height, mip_levels))
+        f.write(bytes(memoryview(blocks).cast("B")) if not hasattr(blocks, "tobytes") else blocks.tobytes())
+
+
+def read_dds(path):
+    """(format, width, height, mip_levels, compressed bytes) of a DDS file."""
+    with open(path, "rb") as f:
+        data = f.read()
+    fmt, w, h, m, off = dds_parse(data)
+    return fmt, w, h, m, data[off:]
