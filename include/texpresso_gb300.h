@@ -274,6 +274,10 @@ TX_API int tx_server_submit(tx_server *server, const tx_server_request *request,
 /* Wait for a job (timeout_ms < 0: no limit) and release it; returns the
  * job's status, or TX_ERR_TIMEOUT with the job still pending. */
 TX_API int tx_server_wait(tx_server *server, uint64_t id, int timeout_ms, tx_server_result *result);
+/* Cancel a job that has not been admitted into device memory yet: returns
+ * TX_OK and its wait then returns TX_ERR_CANCELLED; a job already admitted
+ * returns TX_ERR_BUSY and completes normally. */
+TX_API int tx_server_cancel(tx_server *server, uint64_t id);
 TX_API int tx_server_get_stats(tx_server *server, tx_server_stats *stats);
 /* Finish every queued job, then stop the worker and free the arena. */
 TX_API void tx_server_destroy(tx_server *server);

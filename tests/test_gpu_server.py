@@ -116,3 +116,25 @@ def test_submit_from_many_threads(tx, cuda, oracle):
     for j, out in zip(jobs, results):
         assert np.array_equal(out, _expected(oracle, j))
     srv.close()
+
+
+def test_wait_timeout_and_cancel(tx, cuda):
+    # a 26 MiB budget: the 2048x2048 job (about 24 MiB with mips) fills it,
+    # the 700x700 jobs behind it wait for memory (FIFO admission)
+    big = dict(img=workloads.ramp_texture(2048, 2048, seed=3), w=2048, h=2048, fmt=0, alg=2, aw=False, mips=True)
+    small = [dict(img=workloads.ramp_texture(700, 700, seed=10 + s), w=700, h=700, fmt=2, alg=1, aw=False, mips=True)
+             for s in range(4)]
+    srv = tx.Server(memory_budget=26 << 20, step_blocks=2048, min_share=256)
+    rid, _ = _submit(tx, srv, big)
+    waiting = [_submit(tx, srv, j) for j in small]
+    with pytest.raises(tx.TexpressoError) as e:
+        srv.wait(rid, timeout_ms=0)
+    assert e.value.status == -7                     # still running: timed out, job kept
+    assert srv.cancel(waiting[-1][0]) is True       # queued behind the budget: dropped
+    with pytest.raises(tx.TexpressoError) as e:
+        srv.wait(waiting[-1][0], timeout_ms=60000)
+    assert e.value.status == -11
+    assert srv.wait(rid, timeout_ms=60000)["status"] == 0
+    for i, _ in waiting[:-1]:
+        assert srv.wait(i, timeout_ms=60000)["status"] == 0
+    srv.close()

@@ -360,6 +360,7 @@ _lib.tx_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(_
 _lib.tx_server_submit.argtypes = [_vp, ctypes.POINTER(ServerRequest), ctypes.POINTER(ctypes.c_uint64)]
 _lib.tx_server_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ServerResult)]
 _lib.tx_server_get_stats.argtypes = [_vp, ctypes.POINTER(ServerStats)]
+_lib.tx_server_cancel.argtypes = [_vp, ctypes.c_uint64]
 _lib.tx_server_destroy.argtypes = [_vp]
 _lib.tx_server_destroy.restype = None
 
@@ -410,6 +411,14 @@ class Server:
         _check(rc, "tx_server_wait")
         return {"status": res.status, "levels": res.levels, "steps": res.steps, "blocks": res.blocks,
                 "latency_us": res.latency_us, "queue_us": res.queue_us}
+
+    def cancel(self, rid):
+        """Drop a job not yet admitted (True), or report that it already runs (False)."""
+        rc = _lib.tx_server_cancel(self._h, rid)
+        if rc == -10:
+            return False
+        _check(rc, "tx_server_cancel")
+        return True
 
     def stats(self):
         s = ServerStats()

@@ -6,6 +6,8 @@
 #include "tx_device.cuh"
 #include "tx_internal.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <atomic>
 #include <cstring>
 #include <mutex>
@@ -246,6 +248,10 @@ int tx_compress(int format, const uint8_t *rgba, size_t rgba_len, size_t width, 
     DeviceState *d = nullptr;
     if ((rc = ensure_ready(&d)) != TX_OK) return rc;
     std::lock_guard<std::mutex> lk(d->mu);
+    struct Range {
+        Range() { nvtxRangePushA("tx_compress"); }
+        ~Range() { nvtxRangePop(); }
+    } range;
     cudaError_t e;
     if ((e = grow(&d->d_in, &d->in_cap, in_bytes ? in_bytes : 16)) != cudaSuccess) return fail(e);
     if ((e = grow(&d->d_out, &d->out_cap, output_len)) != cudaSuccess) return fail(e);

@@ -24,6 +24,8 @@
 #include "tx_internal.h"
 #include "tx_batch_internal.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <chrono>
 #include <cstring>
@@ -421,7 +423,10 @@ int tx_batch_create(const tx_batch_item *items, size_t nitems, const tx_batch_tu
 
 int tx_batch_launch(tx_batch *b, void *stream) {
     if (!b) return TX_ERR_INVALID_ARGUMENT;
-    return launch_impl(b, static_cast<cudaStream_t>(stream));
+    nvtxRangePushA("tx_batch_launch");
+    const int rc = launch_impl(b, static_cast<cudaStream_t>(stream));
+    nvtxRangePop();
+    return rc;
 }
 
 int tx_batch_set_tuning(tx_batch *b, const tx_batch_tuning *tuning) {

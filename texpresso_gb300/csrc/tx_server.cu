@@ -20,6 +20,8 @@
 #include "tx_batch_internal.h"
 #include "tx_internal.h"
 
+#include <nvtx3/nvToolsExt.h>
+
 #include <algorithm>
 #include <atomic>
 #include <chrono>
@@ -107,6 +109,8 @@ struct Request {
     int status = TX_OK;
     uint32_t steps = 0;
     std::atomic<bool> finished{false};  // set under tx_server::mu; read by waiters
+    bool cancel = false;                // guarded by tx_server::mu
+    bool admitted = false;              // guarded by tx_server::mu
 };
 
 struct Step {
@@ -183,12 +187,38 @@ void plan_levels(Request *q) {
     for (const Level &lv : q->levels) q->unassigned += lv.nblocks;
 }
 
+void finish_cancelled(tx_server *s, Request *q) {  // caller holds s->mu
+    q->status = TX_ERR_CANCELLED;
+    q->t_done = now_us();
+    q->finished.store(true);
+    s->cv_done.notify_all();
+}
+
 // Admit the head of the waiting line while arena space lasts (FIFO).
 int admit(tx_server *s) {
     while (!s->waiting.empty()) {
         Request *q = s->waiting.front();
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            if (q->cancel) {
+                s->waiting.pop_front();
+                finish_cancelled(s, q);
+                continue;
+            }
+        }
         size_t off = 0;
         if (!s->arena.alloc(q->footprint, &off)) break;
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            if (q->cancel) {  // cancelled between the check and the allocation
+                s->arena.release(off, q->footprint);
+                s->waiting.pop_front();
+                finish_cancelled(s, q);
+                continue;
+            }
+            q->admitted = true;
+        }
+        nvtxRangePushA("tx_server admit");
         s->waiting.pop_front();
         q->arena_off = off;
         q->t_admit = now_us();
@@ -206,6 +236,7 @@ int admit(tx_server *s) {
         }
         if ((e = cudaEventRecord(q->ready_ev, s->s_load)) != cudaSuccess) return fail_server(e);
         s->live.push_back(q);
+        nvtxRangePop();
     }
     return TX_OK;
 }
@@ -272,6 +303,7 @@ int schedule_step(tx_server *s) {
     std::memcpy(st.h_units + n_lane, iter_units.data(), n_team_iter * sizeof(uint2));
     std::memcpy(st.h_units + n_lane + n_team_iter, team_units.data(), n_team * sizeof(uint2));
     cudaError_t e;
+    nvtxRangePushA("tx_server step");
     if ((e = cudaMemcpyAsync(st.d_items, st.h_items, n_items * sizeof(tx::BatchItem), cudaMemcpyHostToDevice,
                              s->s_comp)) != cudaSuccess)
         return fail_server(e);
@@ -284,6 +316,7 @@ int schedule_step(tx_server *s) {
                                      s->s_comp)) != cudaSuccess)
         return fail_server(e);
     if ((e = cudaEventRecord(st.done, s->s_comp)) != cudaSuccess) return fail_server(e);
+    nvtxRangePop();
     st.busy = true;
     s->next_step ^= 1;
     s->step_count++;
@@ -566,6 +599,25 @@ int tx_server_wait(tx_server *s, uint64_t id, int timeout_ms, tx_server_result *
     cudaEventDestroy(q->done_ev);
     delete q;
     return status;
+}
+
+int tx_server_cancel(tx_server *s, uint64_t id) {
+    if (!s) return TX_ERR_INVALID_ARGUMENT;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->requests.find(id);
+    if (it == s->requests.end()) return TX_ERR_INVALID_ARGUMENT;
+    Request *q = it->second;
+    if (q->finished.load()) return q->status == TX_ERR_CANCELLED ? TX_OK : TX_ERR_BUSY;
+    if (q->admitted) return TX_ERR_BUSY;  // already in device memory: it runs to completion
+    for (auto sub = s->submitted.begin(); sub != s->submitted.end(); ++sub) {
+        if (*sub == q) {  // the worker has not seen it yet
+            s->submitted.erase(sub);
+            finish_cancelled(s, q);
+            return TX_OK;
+        }
+    }
+    q->cancel = true;  // waiting for memory: the worker drops it at admission
+    return TX_OK;
 }
 
 int tx_server_get_stats(tx_server *s, tx_server_stats *out) {
