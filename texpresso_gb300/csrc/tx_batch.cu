@@ -40,11 +40,8 @@ cudaError_t upload_batch_tables(const uint32_t lut[4][256][2]) { return upload_t
 template <int TEAM>
 __global__ void __launch_bounds__(256) k_batch_teams(BatchQueue q) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint32_t *tbl = reinterpret_cast<uint32_t *>(smem_raw);
-    load_cand_tables(tbl);
-    TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw + kCandTblBytes);
-    __syncthreads();
-    const uint32_t *tbl4 = tbl, *tbl3 = tbl + kCand4 + 1;
+    TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw);
+    const uint32_t *tbl4 = g_cand, *tbl3 = g_cand + kCand4 + 1;
     const Team<TEAM> tm;
     TeamSmem &sm = teams[threadIdx.x / TEAM];
     for (;;) {

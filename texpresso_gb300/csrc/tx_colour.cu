@@ -21,14 +21,11 @@ __global__ void __launch_bounds__(128) k_range(SrcDesc src, DevParams prm, uint8
 }
 
 template <int FMT, int TEAM, int NITER>
-__global__ void __launch_bounds__(256) k_cluster(SrcDesc src, DevParams prm, uint8_t *__restrict__ out,
+__global__ void __launch_bounds__(256, 4) k_cluster(SrcDesc src, DevParams prm, uint8_t *__restrict__ out,
                                                  size_t nblocks) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    uint32_t *tbl = reinterpret_cast<uint32_t *>(smem_raw);
-    load_cand_tables(tbl);
-    TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw + kCandTblBytes);
-    __syncthreads();
-    const uint32_t *tbl4 = tbl, *tbl3 = tbl + kCand4 + 1;
+    TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw);
+    const uint32_t *tbl4 = g_cand, *tbl3 = g_cand + kCand4 + 1;
     const Team<TEAM> tm;
     const int team_in_cta = threadIdx.x / TEAM;
     const int teams_per_cta = blockDim.x / TEAM;
@@ -39,7 +36,7 @@ __global__ void __launch_bounds__(256) k_cluster(SrcDesc src, DevParams prm, uin
 }
 
 size_t cluster_smem_bytes(int team, int threads) {
-    return kCandTblBytes + (size_t)(threads / team) * sizeof(TeamSmem);
+    return (size_t)(threads / team) * sizeof(TeamSmem);
 }
 
 cudaError_t upload_colour_tables(const uint32_t lut[4][256][2]) { return upload_tables_this_tu(lut); }

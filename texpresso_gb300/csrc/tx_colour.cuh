@@ -26,8 +26,8 @@ namespace tx {
 static __constant__ uint32_t c_lut[4][256][2];
 
 // ClusterFit candidate lists.  Entry bits: 0-3 i (offset of S(0,i)),
-// 4-12 offset of S(i,j), 13-21 offset of S(j,k) (compress4 only),
-// 22-31 rank of (i,j[,k]) in the reference's loop order at 16 colours, so
+// 4-11 offset of S(i,j), 12-19 offset of S(j,k) (compress4 only),
+// 20-29 rank of (i,j[,k]) in the reference's loop order at 16 colours, so
 // comparing entries compares loop positions.
 // Entries are sorted so that the first N[n] are exactly the candidates of an
 // n-colour set (those with max(i+1, j, k) <= n).
@@ -35,19 +35,22 @@ constexpr int kCand4 = 967, kCand3 = 151;
 static __device__ uint32_t g_cand[kCand4 + 1 + kCand3 + 1];
 static __constant__ uint32_t c_ncand4[17];
 static __constant__ uint32_t c_ncand3[17];
-// Weight-lane terms (alpha2, beta2, alphabeta, factor) of every candidate of a
-// 16-colour set whose point weights are all exactly 1: the partial sums' w
-// lanes are then the counts i, j-i, k-j, so the terms depend on the candidate
-// alone.  Filled on the device by k_unit_terms with the same f32 code the
-// sweep would run (wterms4 / wterms3), so loading them is exact.
-static __device__ float4 g_unit4[kCand4 + 1];
-static __device__ float4 g_unit3[kCand3 + 1];
+// The same candidates in the reference's loop order (i, j, k nested), used for
+// 16-colour sets: a round of consecutive candidates then mostly shares S(0,i)
+// and S(i,j) and reads S(j,k) at consecutive addresses.
+static __device__ uint32_t g_cand16[kCand4 + 1 + kCand3 + 1];
+// Lower-bound terms (alpha2, beta2, 2*alphabeta, 1/det) of the g_cand16
+// candidates of a 16-colour set whose weights are all exactly 1 (the w lanes
+// of the partial sums are then the counts i, j-i, k-j): alpha2, beta2,
+// alphabeta are the reference's f32 values, det of those values is evaluated
+// exactly and its reciprocal rounded once (+inf when det <= 0).
+static __device__ float4 g_lb4[kCand4 + 1];
+static __device__ float4 g_lb3[kCand3 + 1];
 
-// Partial-sum table S(a,b), 0 <= a <= b <= 16, stored square with a row
-// stride of 17 float4: the entries that lanes load together (consecutive b,
-// or column b = 16 across rows) fall into different shared-memory banks.
-__host__ __device__ constexpr int sq_idx(int a, int b) { return 17 * a + b; }
-constexpr int kSq = 17 * 17;
+// Partial-sum table S(a,b), 0 <= a <= b <= 16, stored as the upper triangle
+// row by row: S(a,b) at tri_idx(a,b) (153 entries).
+__host__ __device__ constexpr int tri_idx(int a, int b) { return a * (33 - a) / 2 + b; }
+constexpr int kTri = tri_idx(16, 16) + 1;
 
 // ===========================================================================
 // Shared pieces
@@ -367,10 +370,15 @@ struct Team {
 };
 
 struct __align__(16) TeamSmem {
-    float4 S[kSq + 3];      // S(a,b) running sums, S[17a + b] (+pad)
-    float4 PW[16];          // points_weights in the current ordering
+    float4 S[kTri + 3];     // S(a,b) running sums at tri_idx(a,b) (+pad)
+    union {                 // lifetimes do not overlap within an iteration:
+        float LB[kCand4 + 1];   // candidate lower bounds, then the survivor queue
+        struct {
+            float4 PW[16];      // points_weights in the current ordering
+            uint32_t D[16];     // sort keys of the dot products
+        };
+    };
     float P[4][16];         // x, y, z, weight of each point, point order
-    float D[16];            // dot products
     uint32_t hist[8][4];    // orderings of earlier iterations (16 bytes each)
 };
 
@@ -470,18 +478,102 @@ __device__ __forceinline__ float eval3(const float4 p0, const float4 p1, const f
 }
 
 // Decode (i, j, k) from a candidate entry.
-__device__ __forceinline__ void decode_entry(uint32_t e, int &i, int &j, int &k) {
+__host__ __device__ __forceinline__ void decode_entry(uint32_t e, int &i, int &j, int &k) {
     i = (int)(e & 0xFu);
-    j = (int)((e >> 4) & 0x1FFu) - 17 * i;
-    k = (int)((e >> 13) & 0x1FFu) - 17 * j;
+    j = (int)((e >> 4) & 0xFFu) - tri_idx(i, 0);
+    k = (int)((e >> 12) & 0xFFu) - tri_idx(j, 0);
+}
+
+// ---------------------------------------------------------------------------
+// Candidate pruning.  For a candidate with weight-lane terms alpha, beta,
+// gamma (> 0 definite) and per-channel sums ax, bx, the reference's error at
+// any endpoints (a, b) is  sum_c w_c Q_c(a_c, b_c)  with
+//     Q(a, b) = alpha a^2 + beta b^2 + 2 gamma a b - 2 a ax - 2 b bx
+// (cluster.rs:345-353, evaluated in f32).  Q is minimised over all real (a, b)
+// by the unclamped least-squares endpoints, where it equals
+//     -q,  q = (beta ax^2 - 2 gamma ax bx + alpha bx^2) / det,
+// so no clamping or grid snapping can bring the error below -sum_c w_c q_c.
+// The bound is evaluated with cheaper arithmetic than the reference (FMA,
+// ax + bx = x-sum, an approximate reciprocal), and the difference to the
+// reference's f32 error is covered by a margin (weights w_c >= 0, all sums
+// non-negative, W = weight sum, X_c = channel sums, u = 2^-24):
+//   * rounding of the reference's own error evaluation, and using f32
+//     weight-lane terms that differ from its by a few ulps: <= 36 u W sum(w);
+//   * our ax, bx within 16 u X of the reference's, moving q by at most
+//     32 u X (|A*| + |B*|) <= 32 u f W X^2, plus rounding of q, the weighted
+//     sum and f: <= 12 u f W X^2 per channel;
+// so  E_ref >= -f (sum_c w_c q_c + Kb) - eps1  with  Kb = 2^-17 W sum w_c X_c^2
+// and eps1 = 2^-17 W sum w_c (128 u, about three times the derived terms).
+// A candidate whose bound exceeds an error some candidate actually reaches
+// can neither win nor tie, so the exact sweep only needs the others.  The
+// result is the reference's choice bit for bit; only the work changes.
+
+// Bound terms (alpha, beta, 2 gamma, 1/det) from the w lanes of the partial
+// sums, for blocks whose weights are not all 1 (no table entry applies).
+template <int NC>
+__device__ __forceinline__ float4 lb_terms(float p0w, float p1w, float p2w, float xsw) {
+    float al, be, g2;
+    if (NC == 4) {
+        const float p3w = xsw - p0w - p1w - p2w;
+        al = __fmaf_rn(p2w, 1.0f / 9.0f, __fmaf_rn(p1w, 4.0f / 9.0f, p0w));
+        be = __fmaf_rn(p1w, 1.0f / 9.0f, __fmaf_rn(p2w, 4.0f / 9.0f, p3w));
+        g2 = (4.0f / 9.0f) * (p1w + p2w);
+    } else {
+        const float p2r = xsw - p0w - p1w;
+        al = __fmaf_rn(p1w, 0.25f, p0w);
+        be = __fmaf_rn(p1w, 0.25f, p2r);
+        g2 = 0.5f * p1w;
+    }
+    // det = al*be - g*g with the product g*g split exactly (its rounding error
+    // recovered by an FMA), so det carries only the final roundings
+    const float g = 0.5f * g2;
+    const float gg = g * g;
+    const float gerr = __fmaf_rn(g, g, -gg);
+    const float det = __fmaf_rn(al, be, -gg) - gerr;
+    float f;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"(det));
+    return make_float4(al, be, g2, det > 0.0f ? f : __int_as_float(0x7f800000));
+}
+
+// -f (sum_c w_c q_c + kb) - eps1 for one candidate; lt = (alpha, beta, 2 gamma, f).
+template <int NC>
+__device__ __forceinline__ float cand_bound(const float4 p0, const float4 p1, const float4 p2, const float4 xs,
+                                            const float4 lt, const float (&cw)[3], float kb, float eps1) {
+    const float pa[3] = {p0.x, p0.y, p0.z}, pb[3] = {p1.x, p1.y, p1.z}, pc[3] = {p2.x, p2.y, p2.z};
+    const float xsc[3] = {xs.x, xs.y, xs.z};
+    float acc = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float ax = (NC == 4) ? __fmaf_rn(pc[c], 1.0f / 3.0f, __fmaf_rn(pb[c], 2.0f / 3.0f, pa[c]))
+                                   : __fmaf_rn(pb[c], 0.5f, pa[c]);
+        const float bx = xsc[c] - ax;
+        const float u2 = __fmaf_rn(-lt.z, bx, lt.y * ax);
+        const float q = __fmaf_rn(ax, u2, (lt.x * bx) * bx);
+        acc = __fmaf_rn(cw[c], q, acc);
+    }
+    const float v = __fmaf_rn(-lt.w, acc + kb, -eps1);
+    return lt.w <= FLT_MAX ? v : -__int_as_float(0x7f800000);  // no finite bound: keep
+}
+
+// Exact error of the candidate entry e (cluster.rs:189-220, :320-353).
+template <int NC>
+__device__ __forceinline__ float cand_error(const TeamSmem &sm, uint32_t e, const float4 xs, const float (&cw)[3]) {
+    float dummy_a[3], dummy_b[3];
+    const float4 p0 = sm.S[e & 0xFu];
+    const float4 p1 = sm.S[(e >> 4) & 0xFFu];
+    if (NC == 4) {
+        const float4 p2 = sm.S[(e >> 12) & 0xFFu];
+        return eval4<false>(p0, p1, p2, xs, wterms4(p0.w, p1.w, p2.w, xs.w), cw, dummy_a, dummy_b);
+    }
+    return eval3<false>(p0, p1, xs, wterms3(p0.w, p1.w, xs.w), cw, dummy_a, dummy_b);
 }
 
 // ClusterFit::compress3 / compress4 (cluster.rs:152-417) for one team.
 // best_err / best carry the ColourFit state across compress3 -> compress4.
 template <int NC, int TEAM, int NITER>
 __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm, const uint32_t *tbl, int count,
-                                             const float (&principal)[3], const float (&cw)[3], bool valid,
-                                             int my_point, bool unit16, float &best_err, uint2 &best) {
+                                             const float (&principal)[3], const float (&cw)[3], bool prune,
+                                             bool valid, int my_point, bool unit16, float &best_err, uint2 &best) {
     const int lane = tm.lane;
     float run = best_err;
     float ba[3] = {0.0f, 0.0f, 0.0f}, bb[3] = {0.0f, 0.0f, 0.0f};
@@ -497,14 +589,14 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
         float de = FLT_MAX;
         if (lane < count) de = sm.P[0][lane] * axis[0] + sm.P[1][lane] * axis[1] + sm.P[2][lane] * axis[2];
         const uint32_t ke = dps_key(de);
-        if (lane < 16) reinterpret_cast<uint32_t *>(sm.D)[lane] = ke;
+        if (lane < 16) sm.D[lane] = ke;
         tm.sync();
         if (lane < 16) {
             // stable rank: entries with a smaller key, or an equal key earlier
             int rank = 0;
 #pragma unroll
             for (int f = 0; f < 16; ++f) {
-                const uint32_t kf = reinterpret_cast<const uint32_t *>(sm.D)[f];
+                const uint32_t kf = sm.D[f];
                 rank += (kf < ke || (kf == ke && f < lane)) ? 1 : 0;
             }
             reinterpret_cast<uint8_t *>(sm.hist[it])[rank] = (uint8_t)(lane < count ? lane : 0);
@@ -522,11 +614,11 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
         tm.sync();
         // partial sums S(a,b) = pw[a] + ... + pw[b-1], accumulated from zero in
         // loop order exactly like part0/part1/part2 of the reference
-        if (lane == 0) sm.S[sq_idx(count, count)] = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (lane == 0) sm.S[tri_idx(count, count)] = make_float4(0.f, 0.f, 0.f, 0.f);
         if (lane < count) {
             float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-            sm.S[sq_idx(lane, lane)] = acc;
-            const int o = 17 * lane;
+            const int o = tri_idx(lane, 0);
+            sm.S[o + lane] = acc;
             for (int b = lane; b < count; ++b) {
                 const float4 q = sm.PW[b];
                 acc.x += q.x; acc.y += q.y; acc.z += q.z; acc.w += q.w;
@@ -536,37 +628,68 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
         tm.sync();
         xs = sm.S[count];  // S(0, count) == xsum_wsum
 
-        // the sweep: lane-strided over the candidate list
         // (lbest, lent) starts at (run, 0): no entry is below 0, so a candidate
         // that only ties the running best never wins; NaN never compares true
         float lbest = run;
         uint32_t lent = 0;
-        float dummy_a[3], dummy_b[3];
-        if (unit16) {
-            // 16 points of weight 1: the weight-lane terms come from the table
-            const float4 *ut = NC == 4 ? g_unit4 : g_unit3;
+        if (ncand <= 2u * TEAM || !prune) {
+            // short lists: the plain sweep, lane-strided over the candidates
             for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
-                const uint32_t e = tbl[t];
-                const float4 wt = __ldg(ut + t);
-                const float4 p0 = sm.S[e & 0xFu];
-                const float4 p1 = sm.S[(e >> 4) & 0x1FFu];
-                float err;
-                if (NC == 4) err = eval4<false>(p0, p1, sm.S[(e >> 13) & 0x1FFu], xs, wt, cw, dummy_a, dummy_b);
-                else err = eval3<false>(p0, p1, xs, wt, cw, dummy_a, dummy_b);
+                const uint32_t e = __ldg(tbl + t);
+                const float err = cand_error<NC>(sm, e, xs, cw);
                 if (err < lbest || (err == lbest && e < lent)) { lbest = err; lent = e; }
             }
         } else {
+            // 1. a lower bound of every candidate's error (see cand_bound)
+            float x2 = 0.0f;
+            x2 = __fmaf_rn(cw[0], xs.x * xs.x, x2);
+            x2 = __fmaf_rn(cw[1], xs.y * xs.y, x2);
+            x2 = __fmaf_rn(cw[2], xs.z * xs.z, x2);
+            const float kb = 7.62939453125e-6f * xs.w * x2;                     // 2^-17 W sum w X^2
+            const float eps1 = 7.62939453125e-6f * xs.w * (cw[0] + cw[1] + cw[2]);  // 2^-17 W sum w
+            const float4 *lbt = NC == 4 ? g_lb4 : g_lb3;
+            float lmin = __int_as_float(0x7f800000);
+            uint32_t tseed = 0xFFFFFFFFu, eseed = 0;
             for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
-                const uint32_t e = tbl[t];
+                const uint32_t e = __ldg(tbl + t);
                 const float4 p0 = sm.S[e & 0xFu];
-                const float4 p1 = sm.S[(e >> 4) & 0x1FFu];
-                float err;
-                if (NC == 4) {
-                    const float4 p2 = sm.S[(e >> 13) & 0x1FFu];
-                    err = eval4<false>(p0, p1, p2, xs, wterms4(p0.w, p1.w, p2.w, xs.w), cw, dummy_a, dummy_b);
-                } else {
-                    err = eval3<false>(p0, p1, xs, wterms3(p0.w, p1.w, xs.w), cw, dummy_a, dummy_b);
-                }
+                const float4 p1 = sm.S[(e >> 4) & 0xFFu];
+                const float4 p2 = (NC == 4) ? sm.S[(e >> 12) & 0xFFu] : make_float4(0.f, 0.f, 0.f, 0.f);
+                const float4 lt = unit16 ? __ldg(lbt + t) : lb_terms<NC>(p0.w, p1.w, p2.w, xs.w);
+                const float lb = cand_bound<NC>(p0, p1, p2, xs, lt, cw, kb, eps1);
+                sm.LB[t] = lb;
+                if (lb < lmin) { lmin = lb; tseed = t; eseed = e; }
+            }
+            // 2. seeds: every lane's smallest bound, evaluated exactly
+            if (tseed != 0xFFFFFFFFu) {
+                const float err = cand_error<NC>(sm, eseed, xs, cw);
+                if (err < lbest || (err == lbest && eseed < lent)) { lbest = err; lent = eseed; }
+            }
+#pragma unroll
+            for (int off = TEAM / 2; off > 0; off >>= 1) {
+                const float oe = tm.shfl_xor(lbest, off);
+                const uint32_t on = tm.shfl_xor(lent, off);
+                if (oe < lbest || (oe == lbest && on < lent)) { lbest = oe; lent = on; }
+            }
+            // 3. survivors (bound not above the best error reached) are packed in
+            // place into the front of LB; a round only writes slots its own
+            // lanes have already read
+            const float thr = lbest;
+            uint32_t *queue = reinterpret_cast<uint32_t *>(sm.LB);
+            const unsigned below = (1u << lane) - 1u;
+            uint32_t nq = 0;
+            for (uint32_t r0 = 0; r0 < ncand; r0 += TEAM) {
+                const uint32_t t = r0 + (uint32_t)lane;
+                const bool keep = t < ncand && t != tseed && !(sm.LB[t] > thr);
+                const unsigned bits = tm.ballot(keep);
+                if (keep) queue[nq + __popc(bits & below)] = t;
+                nq += (uint32_t)__popc(bits);
+            }
+            tm.sync();
+            // 4. exact errors of the survivors
+            for (uint32_t s = (uint32_t)lane; s < nq; s += TEAM) {
+                const uint32_t e = __ldg(tbl + queue[s]);
+                const float err = cand_error<NC>(sm, e, xs, cw);
                 if (err < lbest || (err == lbest && e < lent)) { lbest = err; lent = e; }
             }
         }
@@ -581,14 +704,15 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
             bentry = lent;
             bit = it;
             const float4 p0 = sm.S[lent & 0xFu];
-            const float4 p1 = sm.S[(lent >> 4) & 0x1FFu];
+            const float4 p1 = sm.S[(lent >> 4) & 0xFFu];
             if (NC == 4) {
-                const float4 p2 = sm.S[(lent >> 13) & 0x1FFu];
+                const float4 p2 = sm.S[(lent >> 12) & 0xFFu];
                 eval4<true>(p0, p1, p2, xs, wterms4(p0.w, p1.w, p2.w, xs.w), cw, ba, bb);
             } else {
                 eval3<true>(p0, p1, xs, wterms3(p0.w, p1.w, xs.w), cw, ba, bb);
             }
         }
+        tm.sync();  // the next ordering reuses the queue's shared memory
         if (bit != it) break;
         axis[0] = bb[0] - ba[0]; axis[1] = bb[1] - ba[1]; axis[2] = bb[2] - ba[2];
     }
@@ -695,12 +819,19 @@ __device__ __forceinline__ uint2 colour_cluster_team(const Team<TEAM> &tm, TeamS
     uint2 best = make_uint2(0u, 0u);
     // 16 distinct colours without alpha weighting: every weight is sqrt(1) = 1
     const bool unit16 = count == 16 && !prm.alpha_weighted;
+    if (count == 16) { tbl4 = g_cand16; tbl3 = g_cand16 + kCand4 + 1; }
+    // the error bound used for pruning holds for finite, non-negative weights
+    const bool prune = cw[0] >= 0.0f && cw[1] >= 0.0f && cw[2] >= 0.0f && cw[0] <= FLT_MAX && cw[1] <= FLT_MAX &&
+                       cw[2] <= FLT_MAX;
     if (FMT == BC1) {
-        cluster_pass<3, TEAM, NITER>(tm, sm, tbl3, count, principal, cw, valid, my_point, unit16, best_err, best);
+        cluster_pass<3, TEAM, NITER>(tm, sm, tbl3, count, principal, cw, prune, valid, my_point, unit16, best_err,
+                                     best);
         if (!transparent)
-            cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, valid, my_point, unit16, best_err, best);
+            cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, prune, valid, my_point, unit16, best_err,
+                                         best);
     } else {
-        cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, valid, my_point, unit16, best_err, best);
+        cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, prune, valid, my_point, unit16, best_err,
+                                     best);
     }
     return best;
 }
@@ -808,27 +939,29 @@ __device__ __forceinline__ void cluster_block(const Team<TEAM> &tm, TeamSmem &sm
     tm.sync();
 }
 
-constexpr int kCandTbl = kCand4 + 1 + kCand3 + 1;
-constexpr size_t kCandTblBytes = (size_t)((kCandTbl * 4 + 15) & ~15);
-
-// Copy the candidate lists of this TU into shared memory (whole CTA).
-__device__ __forceinline__ void load_cand_tables(uint32_t *tbl) {
-    for (int i = threadIdx.x; i < kCandTbl; i += blockDim.x) tbl[i] = g_cand[i];
+// (alpha, beta, 2 gamma, 1/det) of exact weight-lane terms w = (alpha, beta,
+// gamma, factor): det of the f32 values is exact in double (products of two
+// 24-bit significands), and its reciprocal is rounded once to f32.
+__device__ __forceinline__ float4 bound_terms(const float4 w) {
+    const double det = (double)w.x * (double)w.y - (double)w.z * (double)w.z;
+    const float f = det > 0.0 ? (float)(1.0 / det) : __int_as_float(0x7f800000);
+    return make_float4(w.x, w.y, 2.0f * w.z, f);
 }
 
-// Fill g_unit4 / g_unit3 from this TU's candidate lists: the w-lane sums of
-// a 16-point, weight-1 set are S(a,b).w = b - a (exact small integers).
+// Fill the bound terms g_lb4 / g_lb3 from this TU's loop-order candidate
+// lists: the w-lane sums of a 16-point, weight-1 set are S(a,b).w = b - a
+// (exact small integers), and wterms4 / wterms3 are the reference's f32 code.
 static __global__ void k_unit_terms() {
     const int t = blockIdx.x * blockDim.x + threadIdx.x;
     if (t < kCand4) {
         int i, j, k;
-        decode_entry(g_cand[t], i, j, k);
-        g_unit4[t] = wterms4((float)i, (float)(j - i), (float)(k - j), 16.0f);
+        decode_entry(g_cand16[t], i, j, k);
+        g_lb4[t] = bound_terms(wterms4((float)i, (float)(j - i), (float)(k - j), 16.0f));
     }
     if (t < kCand3) {
         int i, j, k;
-        decode_entry(g_cand[kCand4 + 1 + t], i, j, k);
-        g_unit3[t] = wterms3((float)i, (float)(j - i), 16.0f);
+        decode_entry(g_cand16[kCand4 + 1 + t], i, j, k);
+        g_lb3[t] = bound_terms(wterms3((float)i, (float)(j - i), 16.0f));
     }
 }
 
@@ -848,8 +981,8 @@ static inline cudaError_t upload_tables_this_tu(const uint32_t lut[4][256][2]) {
                 const int m = (i + 1 > j ? i + 1 : j) > k ? (i + 1 > j ? i + 1 : j) : k;
                 c4[n4].m = m;
                 c4[n4].rank = n4;
-                c4[n4].e = (uint32_t)i | ((uint32_t)sq_idx(i, j) << 4) | ((uint32_t)sq_idx(j, k) << 13) |
-                           ((uint32_t)n4 << 22);
+                c4[n4].e = (uint32_t)i | ((uint32_t)tri_idx(i, j) << 4) | ((uint32_t)tri_idx(j, k) << 12) |
+                           ((uint32_t)n4 << 20);
                 ++n4;
             }
     for (int i = 0; i < 16; ++i)
@@ -857,10 +990,13 @@ static inline cudaError_t upload_tables_this_tu(const uint32_t lut[4][256][2]) {
             const int m = i + 1 > j ? i + 1 : j;
             c3[n3].m = m;
             c3[n3].rank = n3;
-            c3[n3].e = (uint32_t)i | ((uint32_t)sq_idx(i, j) << 4) | ((uint32_t)n3 << 22);
+            c3[n3].e = (uint32_t)i | ((uint32_t)tri_idx(i, j) << 4) | ((uint32_t)n3 << 20);
             ++n3;
         }
     if (n4 != kCand4 || n3 != kCand3) return cudaErrorInvalidValue;
+    uint32_t loop_tbl[kCand4 + 1 + kCand3 + 1] = {};
+    for (int t = 0; t < kCand4; ++t) loop_tbl[t] = c4[t].e;
+    for (int t = 0; t < kCand3; ++t) loop_tbl[kCand4 + 1 + t] = c3[t].e;
     auto sort_by_m = [](C *v, int n) {
         for (int a = 1; a < n; ++a) {  // stable insertion sort on m
             C t = v[a];
@@ -881,6 +1017,7 @@ static inline cudaError_t upload_tables_this_tu(const uint32_t lut[4][256][2]) {
     }
     cudaError_t e;
     if ((e = cudaMemcpyToSymbol(g_cand, tbl, sizeof(tbl))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(g_cand16, loop_tbl, sizeof(loop_tbl))) != cudaSuccess) return e;
     if ((e = cudaMemcpyToSymbol(c_ncand4, nc4, sizeof(nc4))) != cudaSuccess) return e;
     if ((e = cudaMemcpyToSymbol(c_ncand3, nc3, sizeof(nc3))) != cudaSuccess) return e;
     k_unit_terms<<<(kCand4 + 255) / 256, 256>>>();
