@@ -38,10 +38,13 @@ namespace tx {
 cudaError_t upload_batch_tables(const uint32_t lut[4][256][2]) { return upload_tables_this_tu(lut); }
 
 template <int TEAM>
-__global__ void __launch_bounds__(256) k_batch_teams(BatchQueue q) {
+__global__ void __launch_bounds__(256, 3) k_batch_teams(BatchQueue q) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float s_unorm[256];
+    __shared__ float s_sqrt[17];
+    init_unorm_tables(s_unorm, s_sqrt);
     TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw);
-    const uint32_t *tbl4 = g_cand, *tbl3 = g_cand + kCand4 + 1;
+    const TeamTables tt{g_cand, g_cand + kCand4 + 1, s_unorm, s_sqrt};
     const Team<TEAM> tm;
     TeamSmem &sm = teams[threadIdx.x / TEAM];
     for (;;) {
@@ -58,12 +61,12 @@ __global__ void __launch_bounds__(256) k_batch_teams(BatchQueue q) {
         const int sel = it.format * 2 + (it.kind == KIND_CLUSTER_ITER ? 1 : 0);
         for (uint32_t b = unit.y; b < end; ++b) {
             switch (sel) {
-            case BC1 * 2: cluster_block<BC1, TEAM, 1>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
-            case BC1 * 2 + 1: cluster_block<BC1, TEAM, 8>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
-            case BC2 * 2: cluster_block<BC2, TEAM, 1>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
-            case BC2 * 2 + 1: cluster_block<BC2, TEAM, 8>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
-            case BC3 * 2: cluster_block<BC3, TEAM, 1>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
-            case BC3 * 2 + 1: cluster_block<BC3, TEAM, 8>(tm, sm, tbl4, tbl3, src, b, prm, dst); break;
+            case BC1 * 2: cluster_block<BC1, TEAM, 1>(tm, sm, tt, src, b, prm, dst); break;
+            case BC1 * 2 + 1: cluster_block<BC1, TEAM, 8>(tm, sm, tt, src, b, prm, dst); break;
+            case BC2 * 2: cluster_block<BC2, TEAM, 1>(tm, sm, tt, src, b, prm, dst); break;
+            case BC2 * 2 + 1: cluster_block<BC2, TEAM, 8>(tm, sm, tt, src, b, prm, dst); break;
+            case BC3 * 2: cluster_block<BC3, TEAM, 1>(tm, sm, tt, src, b, prm, dst); break;
+            case BC3 * 2 + 1: cluster_block<BC3, TEAM, 8>(tm, sm, tt, src, b, prm, dst); break;
             default: break;
             }
         }

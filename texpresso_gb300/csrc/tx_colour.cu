@@ -24,15 +24,48 @@ template <int FMT, int TEAM, int NITER>
 __global__ void __launch_bounds__(256, 4) k_cluster(SrcDesc src, DevParams prm, uint8_t *__restrict__ out,
                                                  size_t nblocks) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ float s_unorm[256];
+    __shared__ float s_sqrt[17];
+    __shared__ uint32_t s_next;
+    if (threadIdx.x == 0) s_next = 0;
+    init_unorm_tables(s_unorm, s_sqrt);  // ends with __syncthreads
     TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw);
-    const uint32_t *tbl4 = g_cand, *tbl3 = g_cand + kCand4 + 1;
+    const TeamTables tt{g_cand, g_cand + kCand4 + 1, s_unorm, s_sqrt};
     const Team<TEAM> tm;
-    const int team_in_cta = threadIdx.x / TEAM;
-    const int teams_per_cta = blockDim.x / TEAM;
-    TeamSmem &sm = teams[team_in_cta];
-    const size_t nteams = (size_t)gridDim.x * teams_per_cta;
-    for (size_t b = (size_t)blockIdx.x * teams_per_cta + team_in_cta; b < nblocks; b += nteams)
-        cluster_block<FMT, TEAM, NITER>(tm, sm, tbl4, tbl3, src, b, prm, out);
+    TeamSmem &sm = teams[threadIdx.x / TEAM];
+    if (NITER == 1) {
+        // ClusterFit: team t of CTA c encodes block c * teams + t (grid-strided)
+        const int teams_per_cta = blockDim.x / TEAM;
+        const size_t nteams = (size_t)gridDim.x * teams_per_cta;
+        for (size_t b = (size_t)blockIdx.x * teams_per_cta + threadIdx.x / TEAM; b < nblocks; b += nteams)
+            cluster_block<FMT, TEAM, NITER>(tm, sm, tt, src, b, prm, out);
+        return;
+    }
+    // IterativeClusterFit (persistent CTAs): CTA c owns the chunks of 8
+    // neighbouring blocks c, c + grid, c + 2 grid, ..., and its teams take the
+    // blocks one at a time from a shared counter, so a team that drew cheap
+    // blocks (one colour, one ordering) takes more of them instead of idling
+    // until the CTA's slowest team is done, and teams working at the same time
+    // still read neighbouring pixels.  The next block's pixels are requested
+    // before the current block is encoded.
+    auto take = [&]() {
+        uint32_t k = 0;
+        if (tm.lane == 0) k = atomicAdd(&s_next, 1u);
+        k = tm.shfl(k, 0);
+        return ((size_t)(k >> 3) * gridDim.x + blockIdx.x) * 8u + (k & 7u);
+    };
+    const size_t end_chunk = (nblocks + 7) / 8 * 8;  // slots past this belong to no chunk
+    size_t b = take();
+    TeamPixel tp{0u, false};
+    if (b < nblocks) tp = load_team_pixel(src, b, tm.lane);
+    while (b < end_chunk) {
+        const size_t bn = take();
+        TeamPixel tn{0u, false};
+        if (bn < nblocks) tn = load_team_pixel(src, bn, tm.lane);
+        if (b < nblocks) cluster_block_px<FMT, TEAM, NITER>(tm, sm, tt, tp, b, prm, out);
+        b = bn;
+        tp = tn;
+    }
 }
 
 size_t cluster_smem_bytes(int team, int threads) {
@@ -67,8 +100,26 @@ static cudaError_t launch_cluster_t(const SrcDesc &src, const DevParams &prm, ui
         if (e != cudaSuccess) return e;
         attr_set[dev] = true;
     }
+    // IterativeClusterFit: one wave of persistent CTAs (SMs x resident CTAs),
+    // whose teams deal blocks among themselves, because blocks needing 1 or 2+
+    // orderings differ twofold in cost.  ClusterFit: one chunk per CTA (the
+    // hardware schedules CTAs as slots free up, which measured faster there).
+    static int resident[64] = {};
+    if (NITER > 1 && dev < 64 && resident[dev] == 0) {
+        int sms = 0, per_sm = 0;
+        cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_cluster<FMT, TEAM, NITER>, 256,
+                                                              cluster_smem_bytes(TEAM, 256));
+        if (e != cudaSuccess) return e;
+        resident[dev] = sms * (per_sm > 0 ? per_sm : 1);
+    }
     const size_t teams_per_cta = (size_t)threads / TEAM;
-    size_t grid = (nblocks + teams_per_cta - 1) / teams_per_cta;
+    size_t grid = NITER > 1 ? (nblocks + 7) / 8 : (nblocks + teams_per_cta - 1) / teams_per_cta;  // chunks : blocks
+    if (NITER > 1) {
+        const size_t wave = (size_t)(dev < 64 ? resident[dev] : 1) * (256 / threads);
+        if (grid > wave) grid = wave;
+    }
     if (grid > cfg.max_ctas) grid = cfg.max_ctas;
     if (grid == 0) grid = 1;
     k_cluster<FMT, TEAM, NITER><<<(unsigned)grid, threads, smem, st>>>(src, prm, out, nblocks);

@@ -43,7 +43,7 @@ static __device__ uint32_t g_cand16[kCand4 + 1 + kCand3 + 1];
 // candidates of a 16-colour set whose weights are all exactly 1 (the w lanes
 // of the partial sums are then the counts i, j-i, k-j): alpha2, beta2,
 // alphabeta are the reference's f32 values, det of those values is evaluated
-// exactly and its reciprocal rounded once (+inf when det <= 0).
+// exactly and its reciprocal rounded once (NaN when det <= 0: no bound).
 static __device__ float4 g_lb4[kCand4 + 1];
 static __device__ float4 g_lb3[kCand3 + 1];
 
@@ -532,7 +532,7 @@ __device__ __forceinline__ float4 lb_terms(float p0w, float p1w, float p2w, floa
     const float det = __fmaf_rn(al, be, -gg) - gerr;
     float f;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"(det));
-    return make_float4(al, be, g2, det > 0.0f ? f : __int_as_float(0x7f800000));
+    return make_float4(al, be, g2, det > 0.0f ? f : __int_as_float(0x7fc00000));  // NaN: no bound
 }
 
 // -f (sum_c w_c q_c + kb) - eps1 for one candidate; lt = (alpha, beta, 2 gamma, f).
@@ -551,21 +551,37 @@ __device__ __forceinline__ float cand_bound(const float4 p0, const float4 p1, co
         const float q = __fmaf_rn(ax, u2, (lt.x * bx) * bx);
         acc = __fmaf_rn(cw[c], q, acc);
     }
-    const float v = __fmaf_rn(-lt.w, acc + kb, -eps1);
-    return lt.w <= FLT_MAX ? v : -__int_as_float(0x7f800000);  // no finite bound: keep
+    return __fmaf_rn(-lt.w, acc + kb, -eps1);  // NaN when there is no bound: the candidate is kept
 }
 
-// Exact error of the candidate entry e (cluster.rs:189-220, :320-353).
+// Per-lane best of the candidates a lane evaluated exactly: error, entry and
+// endpoints, compared lexicographically on (error, entry).
+struct LaneBest {
+    float err;
+    uint32_t ent;
+    float a[3], b[3];
+};
+
+// Exact error and endpoints of the candidate entry e (cluster.rs:189-220,
+// :320-353), folded into the lane's best.
 template <int NC>
-__device__ __forceinline__ float cand_error(const TeamSmem &sm, uint32_t e, const float4 xs, const float (&cw)[3]) {
-    float dummy_a[3], dummy_b[3];
+__device__ __forceinline__ void eval_candidate(const TeamSmem &sm, uint32_t e, const float4 xs, const float (&cw)[3],
+                                               LaneBest &lb) {
+    float a[3], b[3], err;
     const float4 p0 = sm.S[e & 0xFu];
     const float4 p1 = sm.S[(e >> 4) & 0xFFu];
     if (NC == 4) {
         const float4 p2 = sm.S[(e >> 12) & 0xFFu];
-        return eval4<false>(p0, p1, p2, xs, wterms4(p0.w, p1.w, p2.w, xs.w), cw, dummy_a, dummy_b);
+        err = eval4<true>(p0, p1, p2, xs, wterms4(p0.w, p1.w, p2.w, xs.w), cw, a, b);
+    } else {
+        err = eval3<true>(p0, p1, xs, wterms3(p0.w, p1.w, xs.w), cw, a, b);
     }
-    return eval3<false>(p0, p1, xs, wterms3(p0.w, p1.w, xs.w), cw, dummy_a, dummy_b);
+    if (err < lb.err || (err == lb.err && e < lb.ent)) {
+        lb.err = err;
+        lb.ent = e;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { lb.a[c] = a[c]; lb.b[c] = b[c]; }
+    }
 }
 
 // ClusterFit::compress3 / compress4 (cluster.rs:152-417) for one team.
@@ -578,7 +594,8 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
     float run = best_err;
     float ba[3] = {0.0f, 0.0f, 0.0f}, bb[3] = {0.0f, 0.0f, 0.0f};
     uint32_t bentry = 0;
-    int bit = 0;
+    int bit = 0, best_rank = 0;
+    bool best_finite = false;
     float axis[3] = {principal[0], principal[1], principal[2]};
     const uint32_t ncand = (NC == 4) ? c_ncand4[count] : c_ncand3[count];
     float4 xs = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -587,6 +604,7 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
     for (int it = 0; it < NITER; ++it) {
         // construct_ordering (cluster.rs:78-136)
         float de = FLT_MAX;
+        int my_rank = 0;
         if (lane < count) de = sm.P[0][lane] * axis[0] + sm.P[1][lane] * axis[1] + sm.P[2][lane] * axis[2];
         const uint32_t ke = dps_key(de);
         if (lane < 16) sm.D[lane] = ke;
@@ -600,7 +618,10 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
                 rank += (kf < ke || (kf == ke && f < lane)) ? 1 : 0;
             }
             reinterpret_cast<uint8_t *>(sm.hist[it])[rank] = (uint8_t)(lane < count ? lane : 0);
+            my_rank = rank;
         }
+        // with every dot product finite, positions 0..count-1 hold each point once
+        const bool finite = tm.ballot(lane < count && ke == 0xFFFFFFFFu) == 0u;
         tm.sync();
         const int my_ord = (lane < 16) ? hist_get(sm, it, lane) : 0;
         bool repeated = false;
@@ -615,30 +636,34 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
         // partial sums S(a,b) = pw[a] + ... + pw[b-1], accumulated from zero in
         // loop order exactly like part0/part1/part2 of the reference
         if (lane == 0) sm.S[tri_idx(count, count)] = make_float4(0.f, 0.f, 0.f, 0.f);
-        if (lane < count) {
+        {
             float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-            const int o = tri_idx(lane, 0);
-            sm.S[o + lane] = acc;
-            for (int b = lane; b < count; ++b) {
-                const float4 q = sm.PW[b];
-                acc.x += q.x; acc.y += q.y; acc.z += q.z; acc.w += q.w;
-                sm.S[o + b + 1] = acc;
+            float4 *row = sm.S + tri_idx(lane < 16 ? lane : 0, 0) + lane;  // &S(lane, lane)
+            if (lane < count) row[0] = acc;
+#pragma unroll
+            for (int s = 0; s < 16; ++s) {
+                if (s >= count) break;
+                if (lane + s < count) {
+                    const float4 q = sm.PW[lane + s];
+                    acc.x += q.x; acc.y += q.y; acc.z += q.z; acc.w += q.w;
+                    row[s + 1] = acc;
+                }
             }
         }
         tm.sync();
         xs = sm.S[count];  // S(0, count) == xsum_wsum
 
-        // (lbest, lent) starts at (run, 0): no entry is below 0, so a candidate
-        // that only ties the running best never wins; NaN never compares true
-        float lbest = run;
-        uint32_t lent = 0;
+        // each lane's best starts at (run, 0): no entry is below 0, so a
+        // candidate that only ties the running best never wins; NaN never
+        // compares true
+        LaneBest ob;
+        ob.err = run;
+        ob.ent = 0;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) { ob.a[c] = 0.0f; ob.b[c] = 0.0f; }
         if (ncand <= 2u * TEAM || !prune) {
             // short lists: the plain sweep, lane-strided over the candidates
-            for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
-                const uint32_t e = __ldg(tbl + t);
-                const float err = cand_error<NC>(sm, e, xs, cw);
-                if (err < lbest || (err == lbest && e < lent)) { lbest = err; lent = e; }
-            }
+            for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) eval_candidate<NC>(sm, __ldg(tbl + t), xs, cw, ob);
         } else {
             // 1. a lower bound of every candidate's error (see cand_bound)
             float x2 = 0.0f;
@@ -649,50 +674,59 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
             const float eps1 = 7.62939453125e-6f * xs.w * (cw[0] + cw[1] + cw[2]);  // 2^-17 W sum w
             const float4 *lbt = NC == 4 ? g_lb4 : g_lb3;
             float lmin = __int_as_float(0x7f800000);
-            uint32_t tseed = 0xFFFFFFFFu, eseed = 0;
+            uint32_t tseed = 0xFFFFFFFFu;
             for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
                 const uint32_t e = __ldg(tbl + t);
                 const float4 p0 = sm.S[e & 0xFu];
                 const float4 p1 = sm.S[(e >> 4) & 0xFFu];
                 const float4 p2 = (NC == 4) ? sm.S[(e >> 12) & 0xFFu] : make_float4(0.f, 0.f, 0.f, 0.f);
                 const float4 lt = unit16 ? __ldg(lbt + t) : lb_terms<NC>(p0.w, p1.w, p2.w, xs.w);
-                const float lb = cand_bound<NC>(p0, p1, p2, xs, lt, cw, kb, eps1);
-                sm.LB[t] = lb;
-                if (lb < lmin) { lmin = lb; tseed = t; eseed = e; }
+                const float bnd = cand_bound<NC>(p0, p1, p2, xs, lt, cw, kb, eps1);
+                sm.LB[t] = bnd;
+                if (bnd < lmin) { lmin = bnd; tseed = t; }
             }
-            // 2. seeds: every lane's smallest bound, evaluated exactly
+            // 2. seeds: every lane's smallest bound, evaluated exactly; the
+            // threshold is the smallest error reached (never above run)
             if (tseed != 0xFFFFFFFFu) {
-                const float err = cand_error<NC>(sm, eseed, xs, cw);
-                if (err < lbest || (err == lbest && eseed < lent)) { lbest = err; lent = eseed; }
+                eval_candidate<NC>(sm, __ldg(tbl + tseed), xs, cw, ob);
+                sm.LB[tseed] = __int_as_float(0x7f800000);  // already evaluated
             }
+            const uint32_t ngroups = (ncand + 3u) >> 2;
+            if (lane == 0)
+                for (uint32_t t = ncand; t < 4u * ngroups; ++t) sm.LB[t] = __int_as_float(0x7f800000);
+            float thr = ob.err;
 #pragma unroll
-            for (int off = TEAM / 2; off > 0; off >>= 1) {
-                const float oe = tm.shfl_xor(lbest, off);
-                const uint32_t on = tm.shfl_xor(lent, off);
-                if (oe < lbest || (oe == lbest && on < lent)) { lbest = oe; lent = on; }
-            }
-            // 3. survivors (bound not above the best error reached) are packed in
-            // place into the front of LB; a round only writes slots its own
-            // lanes have already read
-            const float thr = lbest;
+            for (int off = TEAM / 2; off > 0; off >>= 1) thr = fminf(thr, tm.shfl_xor(thr, off));
+            tm.sync();
+            // 3. survivors (bound not above thr; NaN = no bound) are packed in
+            // place into the front of LB, four bounds per lane and round; a
+            // round only writes slots that have already been read
             uint32_t *queue = reinterpret_cast<uint32_t *>(sm.LB);
+            const float4 *lb4v = reinterpret_cast<const float4 *>(sm.LB);
             const unsigned below = (1u << lane) - 1u;
             uint32_t nq = 0;
-            for (uint32_t r0 = 0; r0 < ncand; r0 += TEAM) {
-                const uint32_t t = r0 + (uint32_t)lane;
-                const bool keep = t < ncand && t != tseed && !(sm.LB[t] > thr);
-                const unsigned bits = tm.ballot(keep);
-                if (keep) queue[nq + __popc(bits & below)] = t;
-                nq += (uint32_t)__popc(bits);
+            for (uint32_t r0 = 0; r0 < ngroups; r0 += TEAM) {
+                const uint32_t g = r0 + (uint32_t)lane;
+                float4 v = make_float4(__int_as_float(0x7f800000), __int_as_float(0x7f800000),
+                                       __int_as_float(0x7f800000), __int_as_float(0x7f800000));
+                if (g < ngroups) v = lb4v[g];
+                const bool k0 = !(v.x > thr), k1 = !(v.y > thr), k2 = !(v.z > thr), k3 = !(v.w > thr);
+                const unsigned b0 = tm.ballot(k0), b1 = tm.ballot(k1), b2 = tm.ballot(k2), b3 = tm.ballot(k3);
+                const uint32_t n0 = (uint32_t)__popc(b0), n1 = (uint32_t)__popc(b1), n2 = (uint32_t)__popc(b2);
+                if (k0) queue[nq + __popc(b0 & below)] = 4u * g;
+                if (k1) queue[nq + n0 + __popc(b1 & below)] = 4u * g + 1u;
+                if (k2) queue[nq + n0 + n1 + __popc(b2 & below)] = 4u * g + 2u;
+                if (k3) queue[nq + n0 + n1 + n2 + __popc(b3 & below)] = 4u * g + 3u;
+                nq += n0 + n1 + n2 + (uint32_t)__popc(b3);
             }
             tm.sync();
             // 4. exact errors of the survivors
-            for (uint32_t s = (uint32_t)lane; s < nq; s += TEAM) {
-                const uint32_t e = __ldg(tbl + queue[s]);
-                const float err = cand_error<NC>(sm, e, xs, cw);
-                if (err < lbest || (err == lbest && e < lent)) { lbest = err; lent = e; }
-            }
+            for (uint32_t s = (uint32_t)lane; s < nq; s += TEAM) eval_candidate<NC>(sm, __ldg(tbl + queue[s]), xs, cw, ob);
         }
+        // lexicographic reduction of the lanes' bests; the winning lane (the
+        // one holding the winning entry) supplies the endpoints
+        float lbest = ob.err;
+        uint32_t lent = ob.ent;
 #pragma unroll
         for (int off = TEAM / 2; off > 0; off >>= 1) {
             const float oe = tm.shfl_xor(lbest, off);
@@ -700,17 +734,14 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
             if (oe < lbest || (oe == lbest && on < lent)) { lbest = oe; lent = on; }
         }
         if (lent != 0u) {
+            const int src = __ffs(tm.ballot(ob.ent == lent)) - 1;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) { ba[c] = tm.shfl(ob.a[c], src); bb[c] = tm.shfl(ob.b[c], src); }
             run = lbest;
             bentry = lent;
             bit = it;
-            const float4 p0 = sm.S[lent & 0xFu];
-            const float4 p1 = sm.S[(lent >> 4) & 0xFFu];
-            if (NC == 4) {
-                const float4 p2 = sm.S[(lent >> 12) & 0xFFu];
-                eval4<true>(p0, p1, p2, xs, wterms4(p0.w, p1.w, p2.w, xs.w), cw, ba, bb);
-            } else {
-                eval3<true>(p0, p1, xs, wterms3(p0.w, p1.w, xs.w), cw, ba, bb);
-            }
+            best_rank = my_rank;
+            best_finite = finite;
         }
         tm.sync();  // the next ordering reuses the queue's shared memory
         if (bit != it) break;
@@ -721,9 +752,14 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
         int i, j, k;
         decode_entry(bentry, i, j, k);
         uint32_t ind = 3;
-        if (valid) {
-            int maxpos = -1;
+        // position of this pixel's point in the winning ordering: its rank, or
+        // (with non-finite dot products) the last position < count holding it
+        int maxpos = tm.shfl(best_rank, my_point >= 0 ? my_point : 0);
+        if (!best_finite) {
+            maxpos = -1;
             for (int m = 0; m < count; ++m) maxpos = (hist_get(sm, bit, m) == my_point) ? m : maxpos;
+        }
+        if (valid) {
             if (NC == 4) ind = maxpos >= k ? 1u : maxpos >= j ? 3u : maxpos >= i ? 2u : 0u;
             else ind = maxpos >= j ? 1u : maxpos >= i ? 2u : 0u;
         }
@@ -734,10 +770,17 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
     }
 }
 
+// Per-CTA inputs of the team path: the candidate lists for sets of fewer than
+// 16 colours and the exact u8 -> [0,1] and sqrt(count) tables in shared memory.
+struct TeamTables {
+    const uint32_t *cand4, *cand3;
+    const float *unorm, *sqrt;
+};
+
 template <int FMT, int TEAM, int NITER>
-__device__ __forceinline__ uint2 colour_cluster_team(const Team<TEAM> &tm, TeamSmem &sm, const uint32_t *tbl4,
-                                                     const uint32_t *tbl3, uint32_t px, bool inb,
-                                                     const DevParams &prm) {
+__device__ __forceinline__ uint2 colour_cluster_team(const Team<TEAM> &tm, TeamSmem &sm, const TeamTables &tt,
+                                                     uint32_t px, bool inb, const DevParams &prm) {
+    const uint32_t *tbl4 = tt.cand4, *tbl3 = tt.cand3;
     const int lane = tm.lane;
     const uint32_t a = px >> 24;
     const bool tr = (FMT == BC1) && inb && a < 128u;
@@ -767,10 +810,10 @@ __device__ __forceinline__ uint2 colour_cluster_team(const Team<TEAM> &tm, TeamS
         }
     }
     if (is_new) {
-        sm.P[0][my_point] = unorm8(px & 0xFFu);
-        sm.P[1][my_point] = unorm8((px >> 8) & 0xFFu);
-        sm.P[2][my_point] = unorm8((px >> 16) & 0xFFu);
-        sm.P[3][my_point] = sqrt_rn(wsum);
+        sm.P[0][my_point] = tt.unorm[px & 0xFFu];
+        sm.P[1][my_point] = tt.unorm[(px >> 8) & 0xFFu];
+        sm.P[2][my_point] = tt.unorm[(px >> 16) & 0xFFu];
+        sm.P[3][my_point] = prm.alpha_weighted ? sqrt_rn(wsum) : tt.sqrt[__popc(eq)];
     }
     tm.sync();
 
@@ -788,29 +831,46 @@ __device__ __forceinline__ uint2 colour_cluster_team(const Team<TEAM> &tm, TeamS
         return (FMT == BC1) ? make_uint2(0u, 0xFFFFFFFFu) : make_uint2(0u, 0u);
     }
 
-    // Sym3x3::weighted_covariance (math.rs:44-73), terms split over lanes
-    float total = 0.0f;
-    for (int k = 0; k < count; ++k) total = total + sm.P[3][k];
-    const int ch = lane < 3 ? lane : 0;
-    float cs = 0.0f;
-    for (int k = 0; k < count; ++k) cs = cs + sm.P[ch][k] * sm.P[3][k];
-    float cen[3] = {tm.shfl(cs, 0), tm.shfl(cs, 1), tm.shfl(cs, 2)};
-    if (total > FLT_EPSILON) { cen[0] = div_rn(cen[0], total); cen[1] = div_rn(cen[1], total); cen[2] = div_rn(cen[2], total); }
-    const int term = lane < 6 ? lane : 0;
-    const int c1 = term < 3 ? 0 : (term < 5 ? 1 : 2);
-    const int c2 = term < 3 ? term : (term < 5 ? term - 2 : 2);
-    const float m1 = c1 == 0 ? cen[0] : (c1 == 1 ? cen[1] : cen[2]);
-    const float m2 = c2 == 0 ? cen[0] : (c2 == 1 ? cen[1] : cen[2]);
-    float cv = 0.0f;
-    for (int k = 0; k < count; ++k) {
-        const float a1 = sm.P[c1][k] - m1;
-        const float a2 = sm.P[c2][k] - m2;
-        const float b2 = a2 * sm.P[3][k];
-        cv += a1 * b2;
+    // Sym3x3::weighted_covariance (math.rs:44-73).  Lane k forms point k's
+    // products; lane t then adds column t in point order, as the reference's
+    // loop does.  Columns are padded with exact zeros to a multiple of 4
+    // (x + 0 == x here: no running sum is -0, so no sign is lost).
+    float *scr = sm.LB;  // free until the candidate sweep: [4][16] then [6][16]
+    const int n4 = (count + 3) & ~3;
+    float px3[3] = {0.f, 0.f, 0.f}, pw = 0.f;
+    if (lane < count) { px3[0] = sm.P[0][lane]; px3[1] = sm.P[1][lane]; px3[2] = sm.P[2][lane]; pw = sm.P[3][lane]; }
+    if (lane < 16) {
+        scr[lane] = px3[0] * pw; scr[16 + lane] = px3[1] * pw; scr[32 + lane] = px3[2] * pw; scr[48 + lane] = pw;
     }
+    tm.sync();
+    const int col = lane < 10 ? lane : 0;
+    auto column_sum = [&](const float *base) {
+        float acc = 0.0f;
+        for (int g = 0; g < n4; g += 4) {
+            const float4 v = *reinterpret_cast<const float4 *>(base + 16 * col + g);
+            acc = acc + v.x; acc = acc + v.y; acc = acc + v.z; acc = acc + v.w;
+        }
+        return acc;
+    };
+    const float sum1 = column_sum(scr);  // lanes 0-2: centroid sums, lane 3: total
+    const float total = tm.shfl(sum1, 3);
+    const float cdiv = total > FLT_EPSILON ? div_rn(sum1, total) : sum1;
+    const float cen[3] = {tm.shfl(cdiv, 0), tm.shfl(cdiv, 1), tm.shfl(cdiv, 2)};
+    if (lane < 16) {
+        const float a0 = px3[0] - cen[0], a1 = px3[1] - cen[1], a2 = px3[2] - cen[2];
+        const float b0 = a0 * pw, b1 = a1 * pw, b2 = a2 * pw;
+        const bool in = lane < count;
+        float *c2 = scr + 64;
+        c2[lane] = in ? a0 * b0 : 0.f;      c2[16 + lane] = in ? a0 * b1 : 0.f;
+        c2[32 + lane] = in ? a0 * b2 : 0.f; c2[48 + lane] = in ? a1 * b1 : 0.f;
+        c2[64 + lane] = in ? a1 * b2 : 0.f; c2[80 + lane] = in ? a2 * b2 : 0.f;
+    }
+    tm.sync();
+    const float cv = column_sum(scr + 64);
     float cov[6];
 #pragma unroll
     for (int t = 0; t < 6; ++t) cov[t] = tm.shfl(cv, t);
+    tm.sync();  // the scratch is reused by the ordering
     float principal[3];
     principle_component(cov, principal);
 
@@ -904,11 +964,56 @@ __device__ __forceinline__ void range_block(const SrcDesc &src, size_t b, const 
     else reinterpret_cast<uint4 *>(out)[b] = make_uint4(al.x, al.y, col.x, col.y);
 }
 
-// Team-per-block: encode and store block b (ClusterFit path).
+// Pixel p of block b for lane p < 16 of a team (RGBA8, pixel order), and
+// whether it lies inside the image / is selected by the block's mask.
+struct TeamPixel {
+    uint32_t px;
+    bool inb;
+};
+
+__device__ __forceinline__ TeamPixel load_team_pixel(const SrcDesc &src, size_t b, int p) {
+    TeamPixel r{0u, false};
+    if (p < 16) {
+        if (src.mode == 1) {
+            r.px = __ldg(reinterpret_cast<const uint32_t *>(src.base + 64 * b) + p);
+            r.inb = src.masks ? ((__ldg(src.masks + b) >> p) & 1u) : true;
+        } else {
+            const uint32_t bx = (uint32_t)(b % src.blocks_wide), by = (uint32_t)(b / src.blocks_wide);
+            const uint32_t x = 4 * bx + (p & 3), y = 4 * by + (p >> 2);
+            r.inb = x < src.width && y < src.height;
+            if (r.inb) r.px = ld_u32_any(src.base + (size_t)y * src.pitch + 4 * (size_t)x);
+        }
+    }
+    return r;
+}
+
+// Team-per-block: encode and store block b (ClusterFit path) from its pixels.
 template <int FMT, int TEAM, int NITER>
-__device__ __forceinline__ void cluster_block(const Team<TEAM> &tm, TeamSmem &sm, const uint32_t *tbl4,
-                                              const uint32_t *tbl3, const SrcDesc &src, size_t b,
-                                              const DevParams &prm, uint8_t *out) {
+__device__ __forceinline__ void cluster_block_px(const Team<TEAM> &tm, TeamSmem &sm, const TeamTables &tt,
+                                                 const TeamPixel tp, size_t b, const DevParams &prm, uint8_t *out) {
+    const int p = tm.lane;
+    const uint32_t px = tp.px;
+    const bool inb = tp.inb;
+    uint2 al = make_uint2(0u, 0u);
+    if (FMT == BC2) {
+        const uint32_t q = inb ? bc2_quant(px >> 24) : 0u;
+        al.x = __reduce_or_sync(tm.mask, p < 8 ? q << (4 * p) : 0u);
+        al.y = __reduce_or_sync(tm.mask, (p >= 8 && p < 16) ? q << (4 * (p - 8)) : 0u);
+    } else if (FMT == BC3) {
+        al = team_bc3_alpha<TEAM>(tm, px >> 24, inb);
+    }
+    const uint2 col = colour_cluster_team<FMT, TEAM, NITER>(tm, sm, tt, px, inb, prm);
+    if (p == 0) {
+        if (FMT == BC1) reinterpret_cast<uint2 *>(out)[b] = col;
+        else reinterpret_cast<uint4 *>(out)[b] = make_uint4(al.x, al.y, col.x, col.y);
+    }
+    tm.sync();
+}
+
+// Team-per-block: load, encode and store block b.
+template <int FMT, int TEAM, int NITER>
+__device__ __forceinline__ void cluster_block(const Team<TEAM> &tm, TeamSmem &sm, const TeamTables &tt,
+                                              const SrcDesc &src, size_t b, const DevParams &prm, uint8_t *out) {
     const int p = tm.lane;
     uint32_t px = 0;
     bool inb = false;
@@ -931,7 +1036,7 @@ __device__ __forceinline__ void cluster_block(const Team<TEAM> &tm, TeamSmem &sm
     } else if (FMT == BC3) {
         al = team_bc3_alpha<TEAM>(tm, px >> 24, inb);
     }
-    const uint2 col = colour_cluster_team<FMT, TEAM, NITER>(tm, sm, tbl4, tbl3, px, inb, prm);
+    const uint2 col = colour_cluster_team<FMT, TEAM, NITER>(tm, sm, tt, px, inb, prm);
     if (p == 0) {
         if (FMT == BC1) reinterpret_cast<uint2 *>(out)[b] = col;
         else reinterpret_cast<uint4 *>(out)[b] = make_uint4(al.x, al.y, col.x, col.y);
@@ -944,7 +1049,7 @@ __device__ __forceinline__ void cluster_block(const Team<TEAM> &tm, TeamSmem &sm
 // 24-bit significands), and its reciprocal is rounded once to f32.
 __device__ __forceinline__ float4 bound_terms(const float4 w) {
     const double det = (double)w.x * (double)w.y - (double)w.z * (double)w.z;
-    const float f = det > 0.0 ? (float)(1.0 / det) : __int_as_float(0x7f800000);
+    const float f = det > 0.0 ? (float)(1.0 / det) : __int_as_float(0x7fc00000);  // NaN: no bound
     return make_float4(w.x, w.y, 2.0f * w.z, f);
 }
 
