@@ -15,8 +15,10 @@ no benchmark inputs.
           pinned host buffers: host->device copy of the RGBA8 input, kernel,
           device->host copy of the blocks, every step.
   roofline  FP32-issue roofline of the ClusterFit kernel (algorithmic FP32
-          operations = reference candidate evaluations x ops per candidate)
-          plus the HBM roofline of the same launch (80 B per block).
+          operations = reference candidate evaluations x ops per candidate;
+          the kernel skips, exactly, the candidates whose error lower bound
+          exceeds an error already reached, so this is a reference-equivalent
+          rate) plus the HBM roofline of the same launch (80 B per block).
   cpu_baseline  the CPU oracle (a C restatement of the reference's block
           path) on all host cores, one block row per task as rayon does.
   extra   the other formats / algorithms of the benchmark configurations,
@@ -392,7 +394,11 @@ def run_ours(args):
         "gpu_launches": launches,
         "roofline": {"bound": "fp32", "achieved": round(achieved_tops, 3), "peak": round(fp32_peak_tops, 2),
                      "unit": "TFLOP/s", "frac": round(achieved_tops / fp32_peak_tops, 4), "traffic": None,
-                     "work": "%d FP32 ops per launch = candidate evaluations x %d (compress4)" % (ops, OPS_CAND4),
+                     "work": "%d FP32 ops per launch = the reference's candidate evaluations x %d (compress4); "
+                             "the kernel bounds every candidate's error from below and evaluates the exact error "
+                             "only where the bound does not exclude it (about 2 %%), so this is the "
+                             "reference-equivalent rate, not the FP32 rate executed (issue-slot use: "
+                             "profiles/k_cluster_bc3_2048.md)" % (ops, OPS_CAND4),
                      "peak_basis": "nominal: 152 SMs x 128 FP32 lanes x %.0f MHz (sm_max_mhz)" % sm_max_mhz},
         "roofline_hbm": {"bound": "hbm", "achieved": round(hbm_achieved, 1), "peak": hbm_peak, "unit": "GB/s",
                          "frac": round(hbm_achieved / hbm_peak, 4), "traffic": None,
