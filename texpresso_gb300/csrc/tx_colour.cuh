@@ -584,12 +584,23 @@ __device__ __forceinline__ void eval_candidate(const TeamSmem &sm, uint32_t e, c
     }
 }
 
+// The ordering along the principal axis is the first ordering of both
+// compress3 and compress4 (cluster.rs:78-136 with the same axis and points),
+// so compress4 takes it and its partial sums from compress3 when compress3
+// built no later ordering over them.
+struct SharedOrder {
+    bool valid;  // S and hist[0] hold the principal-axis ordering
+    int rank;    // this lane's point's position in it
+    bool finite; // every dot product was finite
+};
+
 // ClusterFit::compress3 / compress4 (cluster.rs:152-417) for one team.
 // best_err / best carry the ColourFit state across compress3 -> compress4.
 template <int NC, int TEAM, int NITER>
 __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm, const uint32_t *tbl, int count,
                                              const float (&principal)[3], const float (&cw)[3], bool prune,
-                                             bool valid, int my_point, bool unit16, float &best_err, uint2 &best) {
+                                             bool valid, int my_point, bool unit16, float &best_err, uint2 &best,
+                                             SharedOrder &so) {
     const int lane = tm.lane;
     float run = best_err;
     float ba[3] = {0.0f, 0.0f, 0.0f}, bb[3] = {0.0f, 0.0f, 0.0f};
@@ -603,54 +614,63 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
 #pragma unroll 1
     for (int it = 0; it < NITER; ++it) {
         // construct_ordering (cluster.rs:78-136)
-        float de = FLT_MAX;
         int my_rank = 0;
-        if (lane < count) de = sm.P[0][lane] * axis[0] + sm.P[1][lane] * axis[1] + sm.P[2][lane] * axis[2];
-        const uint32_t ke = dps_key(de);
-        if (lane < 16) sm.D[lane] = ke;
-        tm.sync();
-        if (lane < 16) {
-            // stable rank: entries with a smaller key, or an equal key earlier
-            int rank = 0;
+        bool finite;
+        if (NITER == 1 && so.valid) {  // (the iterative kernel measured faster rebuilding it)
+            my_rank = so.rank;
+            finite = so.finite;
+        } else {
+            float de = FLT_MAX;
+            if (lane < count) de = sm.P[0][lane] * axis[0] + sm.P[1][lane] * axis[1] + sm.P[2][lane] * axis[2];
+            const uint32_t ke = dps_key(de);
+            if (lane < 16) sm.D[lane] = ke;
+            tm.sync();
+            if (lane < 16) {
+                // stable rank: entries with a smaller key, or an equal key earlier
+                int rank = 0;
 #pragma unroll
-            for (int f = 0; f < 16; ++f) {
-                const uint32_t kf = sm.D[f];
-                rank += (kf < ke || (kf == ke && f < lane)) ? 1 : 0;
+                for (int f = 0; f < 16; ++f) {
+                    const uint32_t kf = sm.D[f];
+                    rank += (kf < ke || (kf == ke && f < lane)) ? 1 : 0;
+                }
+                reinterpret_cast<uint8_t *>(sm.hist[it])[rank] = (uint8_t)(lane < count ? lane : 0);
+                my_rank = rank;
             }
-            reinterpret_cast<uint8_t *>(sm.hist[it])[rank] = (uint8_t)(lane < count ? lane : 0);
-            my_rank = rank;
-        }
-        // with every dot product finite, positions 0..count-1 hold each point once
-        const bool finite = tm.ballot(lane < count && ke == 0xFFFFFFFFu) == 0u;
-        tm.sync();
-        const int my_ord = (lane < 16) ? hist_get(sm, it, lane) : 0;
-        bool repeated = false;
+            // with every dot product finite, positions 0..count-1 hold each point once
+            finite = tm.ballot(lane < count && ke == 0xFFFFFFFFu) == 0u;
+            tm.sync();
+            const int my_ord = (lane < 16) ? hist_get(sm, it, lane) : 0;
+            bool repeated = false;
 #pragma unroll 1
-        for (int t = 0; t < it; ++t) repeated |= tm.all(lane >= 16 || hist_get(sm, t, lane) == my_ord);
-        if (repeated) break;
-        if (lane < count) {
-            const float w = sm.P[3][my_ord];
-            sm.PW[lane] = make_float4(sm.P[0][my_ord] * w, sm.P[1][my_ord] * w, sm.P[2][my_ord] * w, 1.0f * w);
-        }
-        tm.sync();
-        // partial sums S(a,b) = pw[a] + ... + pw[b-1], accumulated from zero in
-        // loop order exactly like part0/part1/part2 of the reference
-        if (lane == 0) sm.S[tri_idx(count, count)] = make_float4(0.f, 0.f, 0.f, 0.f);
-        {
-            float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
-            float4 *row = sm.S + tri_idx(lane < 16 ? lane : 0, 0) + lane;  // &S(lane, lane)
-            if (lane < count) row[0] = acc;
+            for (int t = 0; t < it; ++t) repeated |= tm.all(lane >= 16 || hist_get(sm, t, lane) == my_ord);
+            if (repeated) break;
+            if (lane < count) {
+                const float w = sm.P[3][my_ord];
+                sm.PW[lane] = make_float4(sm.P[0][my_ord] * w, sm.P[1][my_ord] * w, sm.P[2][my_ord] * w, 1.0f * w);
+            }
+            tm.sync();
+            // partial sums S(a,b) = pw[a] + ... + pw[b-1], accumulated from zero in
+            // loop order exactly like part0/part1/part2 of the reference
+            if (lane == 0) sm.S[tri_idx(count, count)] = make_float4(0.f, 0.f, 0.f, 0.f);
+            {
+                float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
+                float4 *row = sm.S + tri_idx(lane < 16 ? lane : 0, 0) + lane;  // &S(lane, lane)
+                if (lane < count) row[0] = acc;
 #pragma unroll
-            for (int s = 0; s < 16; ++s) {
-                if (s >= count) break;
-                if (lane + s < count) {
-                    const float4 q = sm.PW[lane + s];
-                    acc.x += q.x; acc.y += q.y; acc.z += q.z; acc.w += q.w;
-                    row[s + 1] = acc;
+                for (int s = 0; s < 16; ++s) {
+                    if (s >= count) break;
+                    if (lane + s < count) {
+                        const float4 q = sm.PW[lane + s];
+                        acc.x += q.x; acc.y += q.y; acc.z += q.z; acc.w += q.w;
+                        row[s + 1] = acc;
+                    }
                 }
             }
+            tm.sync();
+            so.valid = it == 0;
+            so.rank = my_rank;
+            so.finite = finite;
         }
-        tm.sync();
         xs = sm.S[count];  // S(0, count) == xsum_wsum
 
         // each lane's best starts at (run, 0): no entry is below 0, so a
@@ -883,15 +903,16 @@ __device__ __forceinline__ uint2 colour_cluster_team(const Team<TEAM> &tm, TeamS
     // the error bound used for pruning holds for finite, non-negative weights
     const bool prune = cw[0] >= 0.0f && cw[1] >= 0.0f && cw[2] >= 0.0f && cw[0] <= FLT_MAX && cw[1] <= FLT_MAX &&
                        cw[2] <= FLT_MAX;
+    SharedOrder so{false, 0, false};
     if (FMT == BC1) {
         cluster_pass<3, TEAM, NITER>(tm, sm, tbl3, count, principal, cw, prune, valid, my_point, unit16, best_err,
-                                     best);
+                                     best, so);
         if (!transparent)
             cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, prune, valid, my_point, unit16, best_err,
-                                         best);
+                                         best, so);
     } else {
         cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, prune, valid, my_point, unit16, best_err,
-                                     best);
+                                     best, so);
     }
     return best;
 }
