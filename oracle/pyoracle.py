@@ -334,8 +334,9 @@ def cluster_fit(pts, wts, remap, transparent, fmt, weights, iterate):
             P0, P1 = S[0, I], S[I, J]
             P2 = S[J, K] if ncol == 4 else None
             err, A, B = _fit_all(P0, P1, P2, xs, w, ncol)
-            ok = np.where(np.isnan(err) | ~(err < run), np.inf, err)
-            if np.isfinite(ok).any():
+            below = err < run            # NaN never qualifies; -inf does
+            if below.any():
+                ok = np.where(below, err, np.inf)
                 t = int(np.argmin(ok))   # first position of the minimum
                 run, ba, bb, best_it, best_c = ok[t], A[t], B[t], it, cands[t]
             if best_it != it:

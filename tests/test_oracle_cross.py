@@ -8,6 +8,7 @@ import numpy as np
 import pytest
 
 from oracle import pyoracle
+from texpresso_gb300 import workloads
 
 WEIGHTS = [(0.2126, 0.7152, 0.0722), (1.0, 1.0, 1.0), (0.5, 0.0, 2.0)]
 
@@ -65,6 +66,29 @@ def test_restatement_matches_kat(kat):
             got = pyoracle.compress_block_masked(fmt, np.array(d["decoded"], np.uint8), 0xFFFF,
                                                  algos[alg], w, False)
             assert list(got) == d["encoded"], (name, alg)
+
+
+EXTREME_WEIGHTS = [(1.0, 0.0, 0.0), (0.0, 0.0, 0.0), (1e-40, 1.0, 1e-3), (1e6, 1e6, 1e6), (3e38, 1.0, 1.0),
+                   (-1.0, 1.0, 1.0), (float("inf"), 1.0, 1.0), (float("nan"), 1.0, 1.0)]
+
+
+def test_restatements_agree_on_grid_blocks_and_extreme_weights(oracle):
+    """Colours on the 5:6:5 grid and weights that are zero, subnormal, huge,
+    negative or non-finite (errors of -inf or NaN take the reference's
+    "strictly smaller" rule)."""
+    blocks = workloads.grid_blocks(60, seed=3)
+    bad = []
+    with np.errstate(all="ignore"):
+        for w in EXTREME_WEIGHTS:
+            for alg in (0, 1, 2):
+                for fmt in (0, 2):
+                    for i, b in enumerate(blocks):
+                        p = oracle.make_params(alg, w, bool(i % 2))
+                        ref = bytes(oracle.compress_block_masked(fmt, b, 0xFFFF, p))
+                        got = pyoracle.compress_block_masked(fmt, b, 0xFFFF, alg, w, bool(i % 2))
+                        if ref != got:
+                            bad.append((w, alg, fmt, i))
+    assert not bad, bad[:5]
 
 
 def test_cross_check_catches_a_planted_slip(oracle, monkeypatch):

@@ -9,6 +9,7 @@ generators stand in for it).
 * ``value_noise``    -- a smooth multi-octave value-noise field quantised to u8
   with uniform dither, one or two channels (BC4 / BC5 inputs).
 * ``random_blocks``  -- adversarial single blocks for edge-case testing.
+* ``grid_blocks``    -- blocks whose colours lie on the 5:6:5 endpoint grid.
 
 All functions are pure numpy and deterministic for a given seed.
 """
@@ -200,3 +201,24 @@ def mip_reference(img):
     ys1 = np.minimum(2 * np.arange(dh) + 1, h - 1)
     s = (img[ys0][:, xs0].astype(np.uint32) + img[ys0][:, xs1] + img[ys1][:, xs0] + img[ys1][:, xs1])
     return ((s + 2) >> 2).astype(np.uint8)
+
+
+def grid_blocks(n, seed):
+    """Blocks whose colours are 5:6:5 grid values: 2-4 palette entries, or 16
+    entries one grid step apart."""
+    rng = np.random.default_rng(seed)
+    out = np.zeros((n, 16, 4), np.uint8)
+    for b in range(n):
+        k = int(rng.integers(2, 5))
+        pal = np.stack([rng.integers(0, 32, k) * 255 // 31, rng.integers(0, 64, k) * 255 // 63,
+                        rng.integers(0, 32, k) * 255 // 31, rng.integers(0, 256, k)], 1)
+        blk = pal[rng.integers(0, k, 16)]
+        if b % 3 == 0:
+            base = np.array([rng.integers(0, 28), rng.integers(0, 60), rng.integers(0, 28)])
+            steps = np.stack([(base[0] + np.arange(16) % 4), (base[1] + np.arange(16) // 4),
+                              (base[2] + (np.arange(16) % 3))], 1)
+            blk[:, 0] = steps[:, 0] * 255 // 31
+            blk[:, 1] = steps[:, 1] * 255 // 63
+            blk[:, 2] = steps[:, 2] * 255 // 31
+        out[b] = blk
+    return out.reshape(n, 64)
