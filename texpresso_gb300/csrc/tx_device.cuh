@@ -152,45 +152,111 @@ __device__ __forceinline__ uint2 encode_bc2_alpha(const uint32_t (&px)[16], uint
 }
 
 // ---------------------------------------------------------------------------
-// BC3/BC4/BC5 alpha block (lib/src/alpha.rs:70-256) with SIMD-in-word search.
+// BC3/BC4/BC5 alpha block (lib/src/alpha.rs:70-256): codebook search on
+// sorted thresholds, four pixels per 32-bit word (byte c of v[r] = pixel 4r+c).
 //
-// v[r] holds the channel values of pixels 4r..4r+3 (byte c = pixel 4r+c).
-// For every pixel the reference picks the first code with the least squared
-// distance; |v-c| orders codes the same way (and keeps ties), so each 32-bit
-// word tracks four pixels with per-byte min/compare/select.  Errors are sums
-// of squared byte distances (dp4a), which is exact integer arithmetic.
+// fit_codes (alpha.rs:79-117) gives each pixel the first code of least
+// squared distance.  With the 8 codes sorted by (value, index), a code whose
+// value equals its predecessor's can never be chosen (the predecessor has the
+// same distance and a smaller index), so it takes the predecessor's place.
+// Between sorted neighbours a <= b a pixel x prefers b iff 2x > a + b, or
+// 2x == a + b and b's index is smaller, i.e. iff x >= T = (a + b + 2 - [ib < ia]) / 2
+// (integer division).  T never decreases along the sorted list, and the
+// distances are unimodal in it, so the chosen code is the one at position
+// #{j : x >= T_j}, found by a three-step binary search with per-byte
+// compares.  T = 256 only arises between two 255s, which after the merge are
+// the same code, so clamping T to 255 changes nothing.  Squared errors are
+// x^2 - 2xv + v^2 summed with dp4a; the x^2 part is common to both
+// codebooks.
 
-struct AlphaFit {
-    uint32_t err;
-    uint32_t idx[4];  // per-byte code index
+// prmt.b32 in its generic mode: 4-bit selectors, bit 3 replicates the
+// selected byte's sign bit.
+__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+    uint32_t d;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(sel));
+    return d;
+}
+
+// 0xFF in every byte where x >= t (unsigned), else 0x00.
+__device__ __forceinline__ uint32_t bytes_ge(uint32_t x, uint32_t t) {
+    const uint32_t H = 0x80808080u;
+    const uint32_t g = (x | H) - (t & ~H);         // top bit: low 7 bits of x >= those of t
+    const uint32_t m = (x & ~t) | (~(x ^ t) & g);  // top bit: x >= t
+    return prmt(m, 0u, 0xBA98u);                   // replicate each byte's top bit
+}
+
+struct AlphaBook {
+    uint32_t t[7];             // thresholds, replicated in every byte
+    uint32_t idx_lo, idx_hi;   // code index at sorted positions 0-3 / 4-7
+    uint32_t val_lo, val_hi;   // code value at sorted positions 0-3 / 4-7
 };
 
-__device__ __forceinline__ AlphaFit fit_codes8(const uint32_t (&v)[4], const uint32_t (&vm)[4],
-                                               const uint32_t (&codes)[8]) {
-    AlphaFit f;
-    uint32_t best[4];
+__device__ __forceinline__ void cmpx(uint32_t &a, uint32_t &b) {
+    const uint32_t lo = min(a, b), hi = max(a, b);
+    a = lo;
+    b = hi;
+}
+
+// FIVE: codes of the 5-value book (positions known up to the ties of code 6
+// with code 0 and of code 1 with code 7); otherwise any 8 codes.
+template <bool FIVE>
+__device__ __forceinline__ AlphaBook make_book(const uint32_t (&codes)[8]) {
+    uint32_t k[8];  // value << 3 | index
+    if (FIVE) {
+        const int order[8] = {6, 0, 2, 3, 4, 5, 1, 7};
 #pragma unroll
-    for (int r = 0; r < 4; ++r) { best[r] = __vabsdiffu4(v[r], codes[0] * 0x01010101u); f.idx[r] = 0; }
+        for (int j = 0; j < 8; ++j) k[j] = (codes[order[j]] << 3) | (uint32_t)order[j];
+        cmpx(k[0], k[1]);
+        cmpx(k[6], k[7]);
+    } else {
 #pragma unroll
-    for (int j = 1; j < 8; ++j) {
-        const uint32_t c4 = codes[j] * 0x01010101u, j4 = (uint32_t)j * 0x01010101u;
-#pragma unroll
-        for (int r = 0; r < 4; ++r) {
-            uint32_t d = __vabsdiffu4(v[r], c4);
-            uint32_t lt = __vcmpltu4(d, best[r]);
-            best[r] = __vminu4(best[r], d);
-            f.idx[r] = (f.idx[r] & ~lt) | (j4 & lt);
-        }
+        for (int j = 0; j < 8; ++j) k[j] = (codes[j] << 3) | (uint32_t)j;
+        // Batcher's odd-even merge sort of 8
+        cmpx(k[0], k[1]); cmpx(k[2], k[3]); cmpx(k[4], k[5]); cmpx(k[6], k[7]);
+        cmpx(k[0], k[2]); cmpx(k[1], k[3]); cmpx(k[4], k[6]); cmpx(k[5], k[7]);
+        cmpx(k[1], k[2]); cmpx(k[5], k[6]);
+        cmpx(k[0], k[4]); cmpx(k[3], k[7]); cmpx(k[1], k[5]); cmpx(k[2], k[6]);
+        cmpx(k[1], k[4]); cmpx(k[3], k[6]);
+        cmpx(k[2], k[4]); cmpx(k[3], k[5]);
+        cmpx(k[3], k[4]);
     }
-    uint32_t e = 0;
+#pragma unroll
+    for (int j = 1; j < 8; ++j) k[j] = ((k[j] ^ k[j - 1]) < 8u) ? k[j - 1] : k[j];  // equal value: merge
+    AlphaBook bk;
+#pragma unroll
+    for (int j = 0; j < 7; ++j) {
+        const uint32_t a = k[j] >> 3, b = k[j + 1] >> 3;
+        const uint32_t T = min((a + b + 2u - ((k[j + 1] & 7u) < (k[j] & 7u) ? 1u : 0u)) >> 1, 255u);
+        bk.t[j] = T * 0x01010101u;
+    }
+    bk.idx_lo = (k[0] & 7u) | ((k[1] & 7u) << 8) | ((k[2] & 7u) << 16) | ((k[3] & 7u) << 24);
+    bk.idx_hi = (k[4] & 7u) | ((k[5] & 7u) << 8) | ((k[6] & 7u) << 16) | ((k[7] & 7u) << 24);
+    bk.val_lo = (k[0] >> 3) | ((k[1] >> 3) << 8) | ((k[2] >> 3) << 16) | ((k[3] >> 3) << 24);
+    bk.val_hi = (k[4] >> 3) | ((k[5] >> 3) << 8) | ((k[6] >> 3) << 16) | ((k[7] >> 3) << 24);
+    return bk;
+}
+
+// Code index of every pixel (masked pixels: 0) and the book's share of the
+// error, sum over valid pixels of v^2 - 2 x v (the x^2 part is left out).
+__device__ __forceinline__ int fit_book(const uint32_t (&x)[4], const uint32_t (&vm)[4], const AlphaBook &bk,
+                                        uint32_t (&idx)[4]) {
+    uint32_t sv = 0, sxv = 0;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        f.idx[r] &= vm[r];              // masked pixels take code 0 (alpha.rs:92-95)
-        const uint32_t d = best[r] & vm[r];
-        e = __dp4a(d, d, e);
+        const uint32_t m2 = bytes_ge(x[r], bk.t[3]);
+        const uint32_t m1 = bytes_ge(x[r], (m2 & bk.t[5]) | (~m2 & bk.t[1]));
+        const uint32_t hi = (m1 & bk.t[6]) | (~m1 & bk.t[4]);
+        const uint32_t lo = (m1 & bk.t[2]) | (~m1 & bk.t[0]);
+        const uint32_t m0 = bytes_ge(x[r], (m2 & hi) | (~m2 & lo));
+        const uint32_t p = (m2 & 0x04040404u) | (m1 & 0x02020202u) | (m0 & 0x01010101u);
+        const uint32_t q = (p | (p >> 4)) & 0x00FF00FFu;
+        const uint32_t sel = (q | (q >> 8)) & 0xFFFFu;
+        idx[r] = prmt(bk.idx_lo, bk.idx_hi, sel) & vm[r];
+        const uint32_t v = prmt(bk.val_lo, bk.val_hi, sel) & vm[r];
+        sv = __dp4a(v, v, sv);
+        sxv = __dp4a(x[r] & vm[r], v, sxv);
     }
-    f.err = e;
-    return f;
+    return (int)sv - 2 * (int)sxv;
 }
 
 __device__ __forceinline__ uint32_t bytes_min(uint32_t w) {
@@ -250,15 +316,17 @@ __device__ __forceinline__ uint2 encode_bc3_alpha(const uint32_t (&v)[4], uint32
     c7[0] = (uint32_t)min5; c7[1] = (uint32_t)max5;
 #pragma unroll
     for (int i = 1; i < 7; ++i) c7[1 + i] = (uint32_t)(((7 - i) * min7 + i * max7) / 7);
-    const AlphaFit f5 = fit_codes8(v, vm, c5);
-    const AlphaFit f7 = fit_codes8(v, vm, c7);
+    uint32_t i5[4], i7[4];
+    // errors compared without their common x^2 part
+    const int e5 = fit_book(v, vm, make_book<true>(c5), i5);
+    const int e7 = fit_book(v, vm, make_book<false>(c7), i7);
     uint32_t out[4];
-    if (f5.err <= f7.err) {
+    if (e5 <= e7) {
         // write_alpha_block5: a0 > a1 cannot occur after fix_range; kept for fidelity
         if (min5 > max5) {
 #pragma unroll
             for (int r = 0; r < 4; ++r) {
-                uint32_t w = f5.idx[r], o = 0;
+                uint32_t w = i5[r], o = 0;
 #pragma unroll
                 for (int c = 0; c < 4; ++c) {
                     uint32_t x = (w >> (8 * c)) & 0xFFu;
@@ -269,15 +337,15 @@ __device__ __forceinline__ uint2 encode_bc3_alpha(const uint32_t (&v)[4], uint32
             }
             return write_alpha_block((uint32_t)max5, (uint32_t)min5, out);
         }
-        return write_alpha_block((uint32_t)min5, (uint32_t)max5, f5.idx);
+        return write_alpha_block((uint32_t)min5, (uint32_t)max5, i5);
     }
     // write_alpha_block7: min7 < max7 always holds here; 0<->1, x -> 9-x is (9-x)&7
     if (min7 < max7) {
 #pragma unroll
-        for (int r = 0; r < 4; ++r) out[r] = (0x09090909u - f7.idx[r]) & 0x07070707u;
+        for (int r = 0; r < 4; ++r) out[r] = (0x09090909u - i7[r]) & 0x07070707u;
         return write_alpha_block((uint32_t)max7, (uint32_t)min7, out);
     }
-    return write_alpha_block((uint32_t)min7, (uint32_t)max7, f7.idx);
+    return write_alpha_block((uint32_t)min7, (uint32_t)max7, i7);
 }
 
 // Gather one byte channel of 16 RGBA8 pixels into 4 packed words.
