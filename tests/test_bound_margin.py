@@ -1,0 +1,93 @@
+"""The ClusterFit pruning bound (cand_bound / lb_terms in
+texpresso_gb300/csrc/tx_colour.cuh), restated in numpy, never exceeds the
+reference's error (the numpy oracle's f32 evaluation) on any candidate of
+natural, palette and 5:6:5-grid blocks under several weight sets, with and
+without alpha weighting.  FMA steps are emulated in double and rounded once,
+as the device does.  The margin's slack is reported: every candidate must
+keep E - bound >= 0, and the unmargined bound may dip below E only by part of
+the margin."""
+import numpy as np
+
+from oracle import pyoracle as po
+from texpresso_gb300 import workloads
+
+f32 = np.float32
+
+
+def fma(a, b, c):
+    return (np.asarray(a, np.float64) * np.asarray(b, np.float64) + np.asarray(c, np.float64)).astype(np.float32)
+
+
+def bounds(P0, P1, P2, xs, w, nc):
+    """(bound with margin, bound without, margin) per candidate, as the kernel computes them."""
+    if nc == 4:
+        ax = fma(P2[:, :3], f32(1 / 3), fma(P1[:, :3], f32(2 / 3), P0[:, :3]))
+        p3w = (((xs[3] - P0[:, 3]).astype(f32) - P1[:, 3]).astype(f32) - P2[:, 3]).astype(f32)
+        al = fma(P2[:, 3], f32(1 / 9), fma(P1[:, 3], f32(4 / 9), P0[:, 3]))
+        be = fma(P1[:, 3], f32(1 / 9), fma(P2[:, 3], f32(4 / 9), p3w))
+        g2 = (f32(4 / 9) * (P1[:, 3] + P2[:, 3]).astype(f32)).astype(f32)
+    else:
+        ax = fma(P1[:, :3], f32(0.5), P0[:, :3])
+        p2w = ((xs[3] - P0[:, 3]).astype(f32) - P1[:, 3]).astype(f32)
+        al = fma(P1[:, 3], f32(0.25), P0[:, 3])
+        be = fma(P1[:, 3], f32(0.25), p2w)
+        g2 = (f32(0.5) * P1[:, 3]).astype(f32)
+    bx = (xs[:3] - ax).astype(f32)
+    g = (f32(0.5) * g2).astype(f32)
+    det = (al.astype(np.float64) * be - g.astype(np.float64) ** 2).astype(f32)
+    with np.errstate(all="ignore"):
+        f = np.where(det > 0, (f32(1) / det).astype(f32), np.nan).astype(f32)
+        acc = np.zeros(len(al), f32)
+        for c in range(3):
+            u2 = fma(-g2, bx[:, c], (be * ax[:, c]).astype(f32))
+            q = fma(ax[:, c], u2, ((al * bx[:, c]).astype(f32) * bx[:, c]).astype(f32))
+            acc = fma(w[c], q, acc)
+        kb = f32(2.0 ** -17) * xs[3] * f32((w * xs[:3] * xs[:3]).sum())
+        eps1 = f32(2.0 ** -17) * xs[3] * f32(w.sum())
+        lbm = fma(-f, (acc + kb).astype(f32), -eps1)
+        lb0 = (-f * acc).astype(f32)
+        margin = (f * kb + eps1).astype(f32)
+    return lbm, lb0, margin
+
+
+def blocks():
+    img = workloads.ramp_texture(64, 64, seed=9, alpha="ramp")
+    nat = workloads.image_to_blocks(img)[0]
+    return np.concatenate([nat, workloads.grid_blocks(200, seed=10), workloads.random_blocks(150, seed=11)])
+
+
+def test_bound_never_exceeds_reference_error():
+    total, worst = 0, np.inf
+    for bi, blk in enumerate(blocks()):
+        w = [np.array([0.2126, 0.7152, 0.0722], f32), np.array([1, 1, 1], f32),
+             np.array([0.0, 1.0, 0.001], f32)][bi % 3]
+        pts, wts, _, _ = po.colour_set(blk.reshape(16, 4), 0xFFFF, 2, bi % 4 == 3)
+        n = len(pts)
+        if n < 2:
+            continue
+        order = po._order(pts, po.principal(pts, wts))
+        pw = np.zeros((16, 4), f32)
+        for m in range(n):
+            j = order[m]
+            pw[m] = (np.array([pts[j][0], pts[j][1], pts[j][2], 1], f32) * wts[j]).astype(f32)
+        S = np.zeros((17, 17, 4), f32)
+        for a in range(n):
+            S[a, a + 1:n + 1] = np.add.accumulate(pw[a:n], axis=0, dtype=f32)
+        xs = S[0, n]
+        for nc in (4, 3):
+            cands = po._candidates(n, nc)
+            I = np.array([c[0] for c in cands]); J = np.array([c[1] for c in cands])
+            K = np.array([c[2] for c in cands])
+            P0, P1 = S[0, I], S[I, J]
+            P2 = S[J, K] if nc == 4 else np.zeros_like(P0)
+            err, _, _ = po._fit_all(P0, P1, P2 if nc == 4 else None, xs, w, nc)
+            lbm, lb0, margin = bounds(P0, P1, P2, xs, w, nc)
+            ok = np.isfinite(lbm)
+            assert np.all(err[ok] >= lbm[ok]), (bi, nc)
+            total += int(ok.sum())
+            if ok.any():
+                worst = min(worst, float(np.min((err[ok] - lb0[ok]) / margin[ok])))
+    assert total > 100000
+    # the unmargined bound may fall below the error by rounding, never by more
+    # than a small part of the margin
+    assert worst > -0.25, worst
