@@ -7,12 +7,14 @@
 //                     branch-light; a thread owns a block and 32 neighbouring
 //                     blocks load as four coalesced 512-byte rows.
 //   team-per-block    ClusterFit: a team of TEAM lanes (16 or 32) owns a block.
-//                     Lane p owns pixel p for ColourSet; the candidate sweep
-//                     (967 least-squares fits at 16 colours) is spread over the
-//                     team and reduced lexicographically on (error, position in
-//                     the reference's loop order), which selects exactly the
-//                     candidate the sequential "first strictly smaller error"
-//                     loop selects.
+//                     Lane p owns pixel p for ColourSet; the candidates (967
+//                     least-squares fits at 16 colours) are spread over the
+//                     team: each gets a lower bound of its error, only those
+//                     the bound cannot exclude get the reference's exact error
+//                     (see cand_bound), and the lexicographic minimum on (error,
+//                     position in the reference's loop order) selects exactly
+//                     the candidate the sequential "first strictly smaller
+//                     error" loop selects.
 // Both reproduce the reference's f32 operation order (see tx_device.cuh).
 // The constant tables are TU-local: every translation unit that includes this
 // header uploads its own copy with upload_tables_this_tu().
