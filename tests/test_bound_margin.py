@@ -32,20 +32,30 @@ def bounds(P0, P1, P2, xs, w, nc):
         al = fma(P1[:, 3], f32(0.25), P0[:, 3])
         be = fma(P1[:, 3], f32(0.25), p2w)
         g2 = (f32(0.5) * P1[:, 3]).astype(f32)
-    bx = (xs[:3] - ax).astype(f32)
     g = (f32(0.5) * g2).astype(f32)
     det = (al.astype(np.float64) * be - g.astype(np.float64) ** 2).astype(f32)
+    # the quadratic in ax alone (bx = X - ax): A = alpha + beta + 2 gamma, B2 = -2 (alpha + gamma)
+    A = (al.astype(np.float64) + be + g2).astype(f32)
+    B2 = (-(2.0 * al.astype(np.float64) + g2)).astype(f32)
     with np.errstate(all="ignore"):
         f = np.where(det > 0, (f32(1) / det).astype(f32), np.nan).astype(f32)
-        acc = np.zeros(len(al), f32)
+        wx = (w * ax).astype(f32)
+        s1 = (wx[:, 0] * ax[:, 0]).astype(f32)
+        s1 = fma(wx[:, 1], ax[:, 1], s1)
+        s1 = fma(wx[:, 2], ax[:, 2], s1)
+        wX = (w * xs[:3]).astype(f32)
+        s2 = (wX[0] * ax[:, 0]).astype(f32)
+        s2 = fma(wX[1], ax[:, 1], s2)
+        s2 = fma(wX[2], ax[:, 2], s2)
+        Z = f32(0)
         for c in range(3):
-            u2 = fma(-g2, bx[:, c], (be * ax[:, c]).astype(f32))
-            q = fma(ax[:, c], u2, ((al * bx[:, c]).astype(f32) * bx[:, c]).astype(f32))
-            acc = fma(w[c], q, acc)
-        kb = f32(2.0 ** -17) * xs[3] * f32((w * xs[:3] * xs[:3]).sum())
+            Z = fma(w[c], (xs[c] * xs[c]).astype(f32), Z)
+        kb = f32(2.0 ** -17) * xs[3] * Z
         eps1 = f32(2.0 ** -17) * xs[3] * f32(w.sum())
-        lbm = fma(-f, (acc + kb).astype(f32), -eps1)
-        lb0 = (-f * acc).astype(f32)
+        acc = fma(A, s1, fma(B2, s2, fma(al, Z, kb)))
+        lbm = fma(-f, acc, -eps1)
+        acc0 = fma(A, s1, fma(B2, s2, (al * Z).astype(f32)))
+        lb0 = (-f * acc0).astype(f32)
         margin = (f * kb + eps1).astype(f32)
     return lbm, lb0, margin
 

@@ -41,11 +41,10 @@ static __constant__ uint32_t c_ncand3[17];
 // 16-colour sets: a round of consecutive candidates then mostly shares S(0,i)
 // and S(i,j) and reads S(j,k) at consecutive addresses.
 static __device__ uint32_t g_cand16[kCand4 + 1 + kCand3 + 1];
-// Lower-bound terms (alpha2, beta2, 2*alphabeta, 1/det) of the g_cand16
-// candidates of a 16-colour set whose weights are all exactly 1 (the w lanes
-// of the partial sums are then the counts i, j-i, k-j): alpha2, beta2,
-// alphabeta are the reference's f32 values, det of those values is evaluated
-// exactly and its reciprocal rounded once (NaN when det <= 0: no bound).
+// Lower-bound terms (A, -2B, alpha2, 1/det) of the g_cand16 candidates of a
+// 16-colour set whose weights are all exactly 1 (the w lanes of the partial
+// sums are then the counts i, j-i, k-j), from the reference's f32 alpha2,
+// beta2, alphabeta (see bound_terms; NaN when det <= 0: no bound).
 static __device__ float4 g_lb4[kCand4 + 1];
 static __device__ float4 g_lb3[kCand3 + 1];
 
@@ -495,23 +494,27 @@ __host__ __device__ __forceinline__ void decode_entry(uint32_t e, int &i, int &j
 // by the unclamped least-squares endpoints, where it equals
 //     -q,  q = (beta ax^2 - 2 gamma ax bx + alpha bx^2) / det,
 // so no clamping or grid snapping can bring the error below -sum_c w_c q_c.
-// The bound is evaluated with cheaper arithmetic than the reference (FMA,
-// ax + bx = x-sum, an approximate reciprocal), and the difference to the
-// reference's f32 error is covered by a margin (weights w_c >= 0, all sums
-// non-negative, W = weight sum, X_c = channel sums, u = 2^-24):
+// With bx = X - ax (X_c the channel sums) and A = alpha + beta + 2 gamma,
+// B = alpha + gamma, the numerator summed over channels is
+//     sum_c w_c q_c det = A sum_c w_c ax_c^2 - 2B sum_c w_c X_c ax_c + alpha Z,
+// Z = sum_c w_c X_c^2 being the same for every candidate of the block.  The
+// bound is evaluated in that form with cheaper arithmetic than the reference
+// (FMA, an approximate reciprocal), and the difference to the reference's f32
+// error is covered by a margin (weights w_c >= 0, all sums non-negative,
+// W = weight sum, u = 2^-24):
 //   * rounding of the reference's own error evaluation, and using f32
 //     weight-lane terms that differ from its by a few ulps: <= 36 u W sum(w);
-//   * our ax, bx within 16 u X of the reference's, moving q by at most
-//     32 u X (|A*| + |B*|) <= 32 u f W X^2, plus rounding of q, the weighted
-//     sum and f: <= 12 u f W X^2 per channel;
-// so  E_ref >= -f (sum_c w_c q_c + Kb) - eps1  with  Kb = 2^-17 W sum w_c X_c^2
-// and eps1 = 2^-17 W sum w_c (128 u, about three times the derived terms).
+//   * our ax (and X - ax) within 16 u X of the reference's ax, bx, moving the
+//     minimum by at most 32 u X (|A*| + |B*|) <= 32 u f W X^2, plus rounding of
+//     the three sums, their combination and f: <= 26 u f W Z;
+// so  E_ref >= -f (sum_c w_c q_c det + Kb) - eps1  with  Kb = 2^-17 W Z and
+// eps1 = 2^-17 W sum w_c (128 u, about twice the derived terms).
 // A candidate whose bound exceeds an error some candidate actually reaches
 // can neither win nor tie, so the exact sweep only needs the others.  The
 // result is the reference's choice bit for bit; only the work changes.
 
-// Bound terms (alpha, beta, 2 gamma, 1/det) from the w lanes of the partial
-// sums, for blocks whose weights are not all 1 (no table entry applies).
+// Bound terms (A, -2B, alpha, 1/det) from the w lanes of the partial sums, for
+// blocks whose weights are not all 1 (no table entry applies).
 template <int NC>
 __device__ __forceinline__ float4 lb_terms(float p0w, float p1w, float p2w, float xsw) {
     float al, be, g2;
@@ -534,26 +537,48 @@ __device__ __forceinline__ float4 lb_terms(float p0w, float p1w, float p2w, floa
     const float det = __fmaf_rn(al, be, -gg) - gerr;
     float f;
     asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(f) : "f"(det));
-    return make_float4(al, be, g2, det > 0.0f ? f : __int_as_float(0x7fc00000));  // NaN: no bound
+    return make_float4(al + be + g2, -(2.0f * al + g2), al, det > 0.0f ? f : __int_as_float(0x7fc00000));  // NaN: no bound
 }
 
-// -f (sum_c w_c q_c + kb) - eps1 for one candidate; lt = (alpha, beta, 2 gamma, f).
+// Per-block constants of the bound: w_c X_c, Z = sum_c w_c X_c^2, Kb, eps1.
+struct BoundBlock {
+    float wx[3], z, kb, eps1;
+};
+
+__device__ __forceinline__ BoundBlock bound_block(const float4 xs, const float (&cw)[3]) {
+    BoundBlock bb;
+    bb.wx[0] = cw[0] * xs.x;
+    bb.wx[1] = cw[1] * xs.y;
+    bb.wx[2] = cw[2] * xs.z;
+    float z = 0.0f;
+    z = __fmaf_rn(cw[0], xs.x * xs.x, z);
+    z = __fmaf_rn(cw[1], xs.y * xs.y, z);
+    z = __fmaf_rn(cw[2], xs.z * xs.z, z);
+    bb.z = z;
+    bb.kb = 7.62939453125e-6f * xs.w * z;                          // 2^-17 W Z
+    bb.eps1 = 7.62939453125e-6f * xs.w * (cw[0] + cw[1] + cw[2]);  // 2^-17 W sum w
+    return bb;
+}
+
+// -f (A sum w ax^2 - 2B sum w X ax + alpha Z + Kb) - eps1 for one candidate;
+// lt = (A, -2B, alpha, f).
 template <int NC>
-__device__ __forceinline__ float cand_bound(const float4 p0, const float4 p1, const float4 p2, const float4 xs,
-                                            const float4 lt, const float (&cw)[3], float kb, float eps1) {
+__device__ __forceinline__ float cand_bound(const float4 p0, const float4 p1, const float4 p2, const float4 lt,
+                                            const float (&cw)[3], const BoundBlock &bb) {
     const float pa[3] = {p0.x, p0.y, p0.z}, pb[3] = {p1.x, p1.y, p1.z}, pc[3] = {p2.x, p2.y, p2.z};
-    const float xsc[3] = {xs.x, xs.y, xs.z};
-    float acc = 0.0f;
+    float ax[3];
 #pragma unroll
-    for (int c = 0; c < 3; ++c) {
-        const float ax = (NC == 4) ? __fmaf_rn(pc[c], 1.0f / 3.0f, __fmaf_rn(pb[c], 2.0f / 3.0f, pa[c]))
-                                   : __fmaf_rn(pb[c], 0.5f, pa[c]);
-        const float bx = xsc[c] - ax;
-        const float u2 = __fmaf_rn(-lt.z, bx, lt.y * ax);
-        const float q = __fmaf_rn(ax, u2, (lt.x * bx) * bx);
-        acc = __fmaf_rn(cw[c], q, acc);
-    }
-    return __fmaf_rn(-lt.w, acc + kb, -eps1);  // NaN when there is no bound: the candidate is kept
+    for (int c = 0; c < 3; ++c)
+        ax[c] = (NC == 4) ? __fmaf_rn(pc[c], 1.0f / 3.0f, __fmaf_rn(pb[c], 2.0f / 3.0f, pa[c]))
+                          : __fmaf_rn(pb[c], 0.5f, pa[c]);
+    float s1 = (cw[0] * ax[0]) * ax[0];
+    s1 = __fmaf_rn(cw[1] * ax[1], ax[1], s1);
+    s1 = __fmaf_rn(cw[2] * ax[2], ax[2], s1);
+    float s2 = bb.wx[0] * ax[0];
+    s2 = __fmaf_rn(bb.wx[1], ax[1], s2);
+    s2 = __fmaf_rn(bb.wx[2], ax[2], s2);
+    const float acc = __fmaf_rn(lt.x, s1, __fmaf_rn(lt.y, s2, __fmaf_rn(lt.z, bb.z, bb.kb)));
+    return __fmaf_rn(-lt.w, acc, -bb.eps1);  // NaN when there is no bound: the candidate is kept
 }
 
 // Per-lane best of the candidates a lane evaluated exactly: error, entry and
@@ -688,12 +713,7 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
             for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) eval_candidate<NC>(sm, __ldg(tbl + t), xs, cw, ob);
         } else {
             // 1. a lower bound of every candidate's error (see cand_bound)
-            float x2 = 0.0f;
-            x2 = __fmaf_rn(cw[0], xs.x * xs.x, x2);
-            x2 = __fmaf_rn(cw[1], xs.y * xs.y, x2);
-            x2 = __fmaf_rn(cw[2], xs.z * xs.z, x2);
-            const float kb = 7.62939453125e-6f * xs.w * x2;                     // 2^-17 W sum w X^2
-            const float eps1 = 7.62939453125e-6f * xs.w * (cw[0] + cw[1] + cw[2]);  // 2^-17 W sum w
+            const BoundBlock bb = bound_block(xs, cw);
             const float4 *lbt = NC == 4 ? g_lb4 : g_lb3;
             float lmin = __int_as_float(0x7f800000);
             uint32_t tseed = 0xFFFFFFFFu;
@@ -703,7 +723,7 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
                 const float4 p1 = sm.S[(e >> 4) & 0xFFu];
                 const float4 p2 = (NC == 4) ? sm.S[(e >> 12) & 0xFFu] : make_float4(0.f, 0.f, 0.f, 0.f);
                 const float4 lt = unit16 ? __ldg(lbt + t) : lb_terms<NC>(p0.w, p1.w, p2.w, xs.w);
-                const float bnd = cand_bound<NC>(p0, p1, p2, xs, lt, cw, kb, eps1);
+                const float bnd = cand_bound<NC>(p0, p1, p2, lt, cw, bb);
                 sm.LB[t] = bnd;
                 if (bnd < lmin) { lmin = bnd; tseed = t; }
             }
@@ -1067,13 +1087,15 @@ __device__ __forceinline__ void cluster_block(const Team<TEAM> &tm, TeamSmem &sm
     tm.sync();
 }
 
-// (alpha, beta, 2 gamma, 1/det) of exact weight-lane terms w = (alpha, beta,
-// gamma, factor): det of the f32 values is exact in double (products of two
-// 24-bit significands), and its reciprocal is rounded once to f32.
+// (A, -2B, alpha, 1/det) of exact weight-lane terms w = (alpha, beta, gamma,
+// factor), A = alpha + beta + 2 gamma, B = alpha + gamma: det of the f32 values
+// is exact in double (products of two 24-bit significands), A, B and 1/det are
+// rounded once to f32.
 __device__ __forceinline__ float4 bound_terms(const float4 w) {
-    const double det = (double)w.x * (double)w.y - (double)w.z * (double)w.z;
+    const double al = w.x, be = w.y, ga = w.z;
+    const double det = al * be - ga * ga;
     const float f = det > 0.0 ? (float)(1.0 / det) : __int_as_float(0x7fc00000);  // NaN: no bound
-    return make_float4(w.x, w.y, 2.0f * w.z, f);
+    return make_float4((float)(al + be + 2.0 * ga), (float)(-2.0 * (al + ga)), w.x, f);
 }
 
 // Fill the bound terms g_lb4 / g_lb3 from this TU's loop-order candidate
