@@ -753,6 +753,7 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
                                        __int_as_float(0x7f800000), __int_as_float(0x7f800000));
                 if (g < ngroups) v = lb4v[g];
                 const bool k0 = !(v.x > thr), k1 = !(v.y > thr), k2 = !(v.z > thr), k3 = !(v.w > thr);
+                if (tm.ballot(k0 || k1 || k2 || k3) == 0u) continue;  // most rounds hold no survivor
                 const unsigned b0 = tm.ballot(k0), b1 = tm.ballot(k1), b2 = tm.ballot(k2), b3 = tm.ballot(k3);
                 const uint32_t n0 = (uint32_t)__popc(b0), n1 = (uint32_t)__popc(b1), n2 = (uint32_t)__popc(b2);
                 if (k0) queue[nq + __popc(b0 & below)] = 4u * g;
