@@ -383,6 +383,29 @@ struct __align__(16) TeamSmem {
     uint32_t hist[8][4];    // orderings of earlier iterations (16 bytes each)
 };
 
+// Sym3x3::principle_component (math.rs:75-97) for a team: lane c < 3 forms
+// component c of each product M v in the reference's order (row 0 times vx,
+// then row 1 times vy added, then row 2 times vz), and every lane takes the
+// three components by shuffle for the max and the scaling.
+template <int TEAM>
+__device__ __forceinline__ void principle_component_team(const Team<TEAM> &tm, const float (&m)[6], float (&v)[3]) {
+    const int c = tm.lane < 3 ? tm.lane : 0;
+    const float a0 = c == 0 ? m[0] : (c == 1 ? m[1] : m[2]);
+    const float a1 = c == 0 ? m[1] : (c == 1 ? m[3] : m[4]);
+    const float a2 = c == 0 ? m[2] : (c == 1 ? m[4] : m[5]);
+    float vx = 1.0f, vy = 1.0f, vz = 1.0f;
+#pragma unroll 1
+    for (int it = 0; it < 8; ++it) {
+        float w = a0 * vx;
+        w = a1 * vy + w;
+        w = a2 * vz + w;
+        const float wx = tm.shfl(w, 0), wy = tm.shfl(w, 1), wz = tm.shfl(w, 2);
+        const float r = rcp_rn(fmaxf(wx, fmaxf(wy, wz)));
+        vx = wx * r; vy = wy * r; vz = wz * r;
+    }
+    v[0] = vx; v[1] = vy; v[2] = vz;
+}
+
 // Sort key of cluster.rs:90-97 as an unsigned integer: finite values keep
 // their order (-0 and +0 tie), every non-finite value ties after all finite
 // ones.  Comparing keys is comparing with fcmp.
@@ -915,7 +938,7 @@ __device__ __forceinline__ uint2 colour_cluster_team(const Team<TEAM> &tm, TeamS
     for (int t = 0; t < 6; ++t) cov[t] = tm.shfl(cv, t);
     tm.sync();  // the scratch is reused by the ordering
     float principal[3];
-    principle_component(cov, principal);
+    principle_component_team(tm, cov, principal);
 
     const float cw[3] = {prm.w[0], prm.w[1], prm.w[2]};
     float best_err = FLT_MAX;
