@@ -269,3 +269,24 @@ def test_decoders_match_oracle(tx, cuda, oracle):
         for b in range(0, data.size // bs, 17):
             assert np.array_equal(np.frombuffer(f.decompress_block(data[b * bs:(b + 1) * bs]), np.uint8),
                                   oracle.decompress_block(fmt, data[b * bs:(b + 1) * bs]))
+
+
+def test_large_textures(tx, cuda, oracle):
+    """~134 M pixels with sides that are not multiples of 4: 32-bit block
+    counts, grid sizing and the last partial block row and column."""
+    w, h = 16382, 8193
+    rng = np.random.default_rng(12)
+    # RangeFit BC1 on a tiled noisy ramp texture
+    tile = workloads.ramp_texture(1024, 1024, seed=13)
+    rgba = np.ascontiguousarray(np.tile(tile, (9, 17, 1))[:h, :w])
+    rgba[rng.integers(0, h, 64), rng.integers(0, w, 64), 3] = 0  # a few transparent pixels
+    p = tx_params(tx, 0)
+    got = dev_compress(tx, cuda, 0, rgba, p)
+    ref = oracle.compress(0, rgba, w, h, oracle.make_params(0, PERCEPTUAL, False))
+    assert np.array_equal(got, ref), "BC1 RangeFit %dx%d differs" % (w, h)
+    del rgba, got, ref
+    # BC4 from native R8
+    r8 = np.ascontiguousarray(np.tile(workloads.value_noise(1024, 1024, channels=1, seed=14), (9, 17, 1))[:h, :w])
+    got = dev_compress(tx, cuda, 3, r8, tx.Params(), channels=1)
+    ref = oracle.compress(3, workloads.expand_to_rgba(r8), w, h, oracle.make_params())
+    assert np.array_equal(got, ref), "BC4 R8 %dx%d differs" % (w, h)
