@@ -11,7 +11,8 @@ namespace tx {
 // Native single-/two-channel rows: 4 or 8 bytes per block row.
 template <int CH>
 __device__ __forceinline__ uint32_t load_block_native(const SrcDesc &s, size_t b, uint32_t (&r8)[4], uint32_t (&g8)[4]) {
-    const uint32_t bx = (uint32_t)(b % s.blocks_wide), by = (uint32_t)(b / s.blocks_wide);
+    uint32_t bx, by;
+    block_coords(s, b, bx, by);
     const uint32_t x0 = 4 * bx;
     uint32_t mask = 0;
 #pragma unroll

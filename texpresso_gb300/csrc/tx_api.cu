@@ -280,7 +280,7 @@ int tx_compress(int format, const uint8_t *rgba, size_t rgba_len, size_t width, 
         src.pitch = pitch;
         src.width = (uint32_t)width;
         src.height = (uint32_t)(height > y0 ? height - y0 : 0);
-        src.blocks_wide = (uint32_t)bw;
+        tx::set_blocks_wide(src, (uint32_t)bw);
         src.channels = 4;
         src.vec16 = (pitch % 16 == 0) ? 1 : 0;
         src.mode = 0;
@@ -351,7 +351,7 @@ int tx_compress_device(int format, const void *src_ptr, size_t src_pitch, int ch
     src.pitch = src_pitch;
     src.width = (uint32_t)width;
     src.height = (uint32_t)height;
-    src.blocks_wide = (uint32_t)tx_num_blocks(width);
+    tx::set_blocks_wide(src, (uint32_t)tx_num_blocks(width));
     src.channels = channels;
     const size_t vec_align = channels == 4 ? 16 : (size_t)channels * 4;
     src.vec16 = ((reinterpret_cast<uintptr_t>(src_ptr) % vec_align) == 0 && (src_pitch % vec_align) == 0) ? 1 : 0;

@@ -385,7 +385,7 @@ int tx_batch_create(const tx_batch_item *items, size_t nitems, const tx_batch_tu
         d.src.pitch = it.src_pitch;
         d.src.width = it.width;
         d.src.height = it.height;
-        d.src.blocks_wide = (uint32_t)tx_num_blocks(it.width);
+        tx::set_blocks_wide(d.src, (uint32_t)tx_num_blocks(it.width));
         d.src.channels = it.channels;
         const size_t va = it.channels == 4 ? 16 : (size_t)it.channels * 4;
         d.src.vec16 = ((reinterpret_cast<uintptr_t>(it.src) % va) == 0 && (it.src_pitch % va) == 0) ? 1 : 0;
@@ -665,7 +665,7 @@ extern "C" int tx_batch_launch_noalloc(const tx_batch_item *items, size_t nitems
             d.src.pitch = it.src_pitch;
             d.src.width = it.width;
             d.src.height = it.height;
-            d.src.blocks_wide = (uint32_t)tx_num_blocks(it.width);
+            tx::set_blocks_wide(d.src, (uint32_t)tx_num_blocks(it.width));
             d.src.channels = it.channels;
             const size_t va = it.channels == 4 ? 16 : (size_t)it.channels * 4;
             d.src.vec16 = ((reinterpret_cast<uintptr_t>(it.src) % va) == 0 && (it.src_pitch % va) == 0) ? 1 : 0;
@@ -750,7 +750,7 @@ void fill_batch_item(const tx_batch_item &it, BatchItem *d) {
     d->src.pitch = it.src_pitch;
     d->src.width = it.width;
     d->src.height = it.height;
-    d->src.blocks_wide = (uint32_t)tx_num_blocks(it.width);
+    tx::set_blocks_wide(d->src, (uint32_t)tx_num_blocks(it.width));
     d->src.channels = it.channels;
     const size_t va = it.channels == 4 ? 16 : (size_t)it.channels * 4;
     d->src.vec16 = ((reinterpret_cast<uintptr_t>(it.src) % va) == 0 && (it.src_pitch % va) == 0) ? 1 : 0;

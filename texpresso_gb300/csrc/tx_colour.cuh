@@ -1045,7 +1045,8 @@ __device__ __forceinline__ TeamPixel load_team_pixel(const SrcDesc &src, size_t 
             r.px = __ldg(reinterpret_cast<const uint32_t *>(src.base + 64 * b) + p);
             r.inb = src.masks ? ((__ldg(src.masks + b) >> p) & 1u) : true;
         } else {
-            const uint32_t bx = (uint32_t)(b % src.blocks_wide), by = (uint32_t)(b / src.blocks_wide);
+            uint32_t bx, by;
+            block_coords(src, b, bx, by);
             const uint32_t x = 4 * bx + (p & 3), y = 4 * by + (p >> 2);
             r.inb = x < src.width && y < src.height;
             if (r.inb) r.px = ld_u32_any(src.base + (size_t)y * src.pitch + 4 * (size_t)x);
@@ -1089,7 +1090,8 @@ __device__ __forceinline__ void cluster_block(const Team<TEAM> &tm, TeamSmem &sm
             px = __ldg(reinterpret_cast<const uint32_t *>(src.base + 64 * b) + p);
             inb = src.masks ? ((__ldg(src.masks + b) >> p) & 1u) : true;
         } else {
-            const uint32_t bx = (uint32_t)(b % src.blocks_wide), by = (uint32_t)(b / src.blocks_wide);
+            uint32_t bx, by;
+            block_coords(src, b, bx, by);
             const uint32_t x = 4 * bx + (p & 3), y = 4 * by + (p >> 2);
             inb = x < src.width && y < src.height;
             if (inb) px = ld_u32_any(src.base + (size_t)y * src.pitch + 4 * (size_t)x);

@@ -29,10 +29,56 @@ struct SrcDesc {
     size_t pitch;          // mode 0: bytes between rows
     uint32_t width, height;
     uint32_t blocks_wide;  // num_blocks(width)
+    uint32_t bw_magic, bw_shift, bw_flags;  // division by blocks_wide (set_blocks_wide)
     int channels;          // 4 = RGBA8, 1 = R8, 2 = RG8
     int vec16;             // mode 0, RGBA8: rows 16-byte aligned -> 128-bit loads
     int mode;              // 0 image, 1 block list
 };
+
+// blocks_wide and the multiplier that divides 32-bit block numbers by it:
+// q = umulhi(n, magic) >> shift, or with the add step (flags bit 0)
+// q = (((n - t) >> 1) + t) >> shift, t = umulhi(n, magic), or n >> shift for a
+// power of two (flags bit 1) -- division by an invariant integer with a
+// rounded-up reciprocal (Granlund and Montgomery), exact for every 32-bit n.
+inline void set_blocks_wide(SrcDesc &s, uint32_t bw) {
+    s.blocks_wide = bw;
+    s.bw_magic = 0;
+    s.bw_shift = 0;
+    s.bw_flags = 2;
+    if (bw == 0) return;
+    const uint32_t l = 31u - (uint32_t)__builtin_clz(bw);
+    s.bw_shift = l;
+    if ((bw & (bw - 1)) == 0) return;
+    const uint64_t num = (uint64_t)1 << (32 + l);
+    uint64_t m = num / bw;
+    const uint64_t rem = num - m * bw;
+    if (bw - rem < ((uint64_t)1 << l)) {
+        s.bw_flags = 0;
+    } else {
+        m = 2 * m + (2 * rem >= bw ? 1u : 0u);
+        s.bw_flags = 1;
+    }
+    s.bw_magic = (uint32_t)(m + 1);
+}
+
+// Block column and row of block b.
+__device__ __forceinline__ void block_coords(const SrcDesc &s, size_t b, uint32_t &bx, uint32_t &by) {
+    if (b <= 0xFFFFFFFFull) {
+        const uint32_t n = (uint32_t)b;
+        uint32_t q;
+        if (s.bw_flags & 2u) {
+            q = n >> s.bw_shift;
+        } else {
+            const uint32_t t = __umulhi(n, s.bw_magic);
+            q = (s.bw_flags & 1u) ? ((((n - t) >> 1) + t) >> s.bw_shift) : (t >> s.bw_shift);
+        }
+        by = q;
+        bx = n - q * s.blocks_wide;
+    } else {
+        by = (uint32_t)(b / s.blocks_wide);
+        bx = (uint32_t)(b % s.blocks_wide);
+    }
+}
 
 __host__ __device__ constexpr int block_bytes(int fmt) { return (fmt == BC1 || fmt == BC4) ? 8 : 16; }
 
@@ -102,7 +148,8 @@ __device__ __forceinline__ uint32_t load_block_rgba(const SrcDesc &s, size_t b, 
         }
         return s.masks ? (__ldg(s.masks + b) & 0xFFFFu) : 0xFFFFu;
     }
-    const uint32_t bx = (uint32_t)(b % s.blocks_wide), by = (uint32_t)(b / s.blocks_wide);
+    uint32_t bx, by;
+    block_coords(s, b, bx, by);
     const uint32_t x0 = 4 * bx;
     uint32_t mask = 0;
 #pragma unroll
