@@ -224,6 +224,18 @@ __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
     return d;
 }
 
+// Lane-wise minimum / maximum of two pairs of unsigned 16-bit values.
+__device__ __forceinline__ uint32_t min_u16x2(uint32_t a, uint32_t b) {
+    uint32_t d;
+    asm("min.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+__device__ __forceinline__ uint32_t max_u16x2(uint32_t a, uint32_t b) {
+    uint32_t d;
+    asm("max.u16x2 %0, %1, %2;" : "=r"(d) : "r"(a), "r"(b));
+    return d;
+}
+
 // 0xFF in every byte where x >= t (unsigned), else 0x00.
 __device__ __forceinline__ uint32_t bytes_ge(uint32_t x, uint32_t t) {
     const uint32_t H = 0x80808080u;
@@ -306,17 +318,6 @@ __device__ __forceinline__ int fit_book(const uint32_t (&x)[4], const uint32_t (
     return (int)sv - 2 * (int)sxv;
 }
 
-__device__ __forceinline__ uint32_t bytes_min(uint32_t w) {
-    w = __vminu4(w, w >> 16);
-    w = __vminu4(w, w >> 8);
-    return w & 0xFFu;
-}
-__device__ __forceinline__ uint32_t bytes_max(uint32_t w) {
-    w = __vmaxu4(w, w >> 16);
-    w = __vmaxu4(w, w >> 8);
-    return w & 0xFFu;
-}
-
 // fix_range (alpha.rs:70-77); min <= max on entry.
 __device__ __forceinline__ void fix_range(int &mn, int &mx, int steps) {
     if (mx - mn < steps) mx = min(mn + steps, 255);
@@ -339,17 +340,27 @@ __device__ __forceinline__ uint2 encode_bc3_alpha(const uint32_t (&v)[4], uint32
     uint32_t vm[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) vm[r] = nibble_to_bytemask((mask >> (4 * r)) & 0xFu);
+    // Ranges (alpha.rs:194-212).  Masked pixels enter as 255 for the minima and
+    // 0 for the maxima (the initial values).  min5 skips zeros: the minimum of
+    // (x - 1) mod 256 plus one, where a zero becomes 255 and a masked pixel
+    // 254 (= 255, the initial value); max5 skips 255s the same way with
+    // (x + 1) mod 256.  Bytes are compared as even and odd 16-bit pairs.
+    const uint32_t H = 0x80808080u;
     uint32_t mn7 = 0xFFFFFFFFu, mx7 = 0, mn5 = 0xFFFFFFFFu, mx5 = 0;
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-        const uint32_t is0 = __vcmpeq4(v[r], 0u), is255 = __vcmpeq4(v[r], 0xFFFFFFFFu);
-        mn7 = __vminu4(mn7, v[r] | ~vm[r]);
-        mx7 = __vmaxu4(mx7, v[r] & vm[r]);
-        mn5 = __vminu4(mn5, v[r] | ~vm[r] | is0);
-        mx5 = __vmaxu4(mx5, v[r] & vm[r] & ~is255);
+        const uint32_t lo7 = v[r] | ~vm[r], hi7 = v[r] & vm[r];
+        const uint32_t lo5 = ((lo7 | H) - 0x01010101u) ^ (~lo7 & H);  // bytewise x - 1 mod 256
+        const uint32_t hi5 = ((hi7 & ~H) + 0x01010101u) ^ (hi7 & H);  // bytewise x + 1 mod 256
+        mn7 = min_u16x2(min_u16x2(mn7, prmt(lo7, 0u, 0x4240u)), prmt(lo7, 0u, 0x4341u));
+        mx7 = max_u16x2(max_u16x2(mx7, prmt(hi7, 0u, 0x4240u)), prmt(hi7, 0u, 0x4341u));
+        mn5 = min_u16x2(min_u16x2(mn5, prmt(lo5, 0u, 0x4240u)), prmt(lo5, 0u, 0x4341u));
+        mx5 = max_u16x2(max_u16x2(mx5, prmt(hi5, 0u, 0x4240u)), prmt(hi5, 0u, 0x4341u));
     }
-    int min7 = (int)bytes_min(mn7), max7 = (int)bytes_max(mx7);
-    int min5 = (int)bytes_min(mn5), max5 = (int)bytes_max(mx5);
+    int min7 = (int)min(mn7 & 0xFFFFu, mn7 >> 16), max7 = (int)max(mx7 & 0xFFFFu, mx7 >> 16);
+    int min5 = min((int)min(mn5 & 0xFFFFu, mn5 >> 16) + 1, 255);
+    const int m5 = (int)max(mx5 & 0xFFFFu, mx5 >> 16);
+    int max5 = m5 > 0 ? m5 - 1 : 0;
     if (min5 > max5) min5 = max5;
     if (min7 > max7) min7 = max7;
     fix_range(min5, max5, 5);
