@@ -256,29 +256,20 @@ __device__ __forceinline__ void cmpx(uint32_t &a, uint32_t &b) {
     b = hi;
 }
 
-// FIVE: codes of the 5-value book (positions known up to the ties of code 6
-// with code 0 and of code 1 with code 7); otherwise any 8 codes.
-template <bool FIVE>
+// Book of any 8 codes (the 7-value book: codes 0 and 1 are min5 and max5,
+// alpha.rs:237-239, anywhere among the interpolants of min7..max7).
 __device__ __forceinline__ AlphaBook make_book(const uint32_t (&codes)[8]) {
     uint32_t k[8];  // value << 3 | index
-    if (FIVE) {
-        const int order[8] = {6, 0, 2, 3, 4, 5, 1, 7};
 #pragma unroll
-        for (int j = 0; j < 8; ++j) k[j] = (codes[order[j]] << 3) | (uint32_t)order[j];
-        cmpx(k[0], k[1]);
-        cmpx(k[6], k[7]);
-    } else {
-#pragma unroll
-        for (int j = 0; j < 8; ++j) k[j] = (codes[j] << 3) | (uint32_t)j;
-        // Batcher's odd-even merge sort of 8
-        cmpx(k[0], k[1]); cmpx(k[2], k[3]); cmpx(k[4], k[5]); cmpx(k[6], k[7]);
-        cmpx(k[0], k[2]); cmpx(k[1], k[3]); cmpx(k[4], k[6]); cmpx(k[5], k[7]);
-        cmpx(k[1], k[2]); cmpx(k[5], k[6]);
-        cmpx(k[0], k[4]); cmpx(k[3], k[7]); cmpx(k[1], k[5]); cmpx(k[2], k[6]);
-        cmpx(k[1], k[4]); cmpx(k[3], k[6]);
-        cmpx(k[2], k[4]); cmpx(k[3], k[5]);
-        cmpx(k[3], k[4]);
-    }
+    for (int j = 0; j < 8; ++j) k[j] = (codes[j] << 3) | (uint32_t)j;
+    // Batcher's odd-even merge sort of 8
+    cmpx(k[0], k[1]); cmpx(k[2], k[3]); cmpx(k[4], k[5]); cmpx(k[6], k[7]);
+    cmpx(k[0], k[2]); cmpx(k[1], k[3]); cmpx(k[4], k[6]); cmpx(k[5], k[7]);
+    cmpx(k[1], k[2]); cmpx(k[5], k[6]);
+    cmpx(k[0], k[4]); cmpx(k[3], k[7]); cmpx(k[1], k[5]); cmpx(k[2], k[6]);
+    cmpx(k[1], k[4]); cmpx(k[3], k[6]);
+    cmpx(k[2], k[4]); cmpx(k[3], k[5]);
+    cmpx(k[3], k[4]);
 #pragma unroll
     for (int j = 1; j < 8; ++j) k[j] = ((k[j] ^ k[j - 1]) < 8u) ? k[j - 1] : k[j];  // equal value: merge
     AlphaBook bk;
@@ -292,6 +283,26 @@ __device__ __forceinline__ AlphaBook make_book(const uint32_t (&codes)[8]) {
     bk.idx_hi = (k[4] & 7u) | ((k[5] & 7u) << 8) | ((k[6] & 7u) << 16) | ((k[7] & 7u) << 24);
     bk.val_lo = (k[0] >> 3) | ((k[1] >> 3) << 8) | ((k[2] >> 3) << 16) | ((k[3] >> 3) << 24);
     bk.val_hi = (k[4] >> 3) | ((k[5] >> 3) << 8) | ((k[6] >> 3) << 16) | ((k[7] >> 3) << 24);
+    return bk;
+}
+
+// The 5-value book (alpha.rs:227-234) needs no sort: its values run
+// 0 (index 6), min5 (0), the four interpolants (2-5), max5 (1), 255 (7), with
+// the interpolants strictly between min5 and max5 after fix_range.  The
+// thresholds follow from the rule above with the index comparisons known; a
+// min5 of 0 gets threshold 0 (index 0 always beats index 6), and a max5 of 255
+// makes the last position index 1 again (the merge of equal values).
+__device__ __forceinline__ AlphaBook make_book5(uint32_t min5, uint32_t max5, const uint32_t (&c)[8]) {
+    AlphaBook bk;
+    const uint32_t t[7] = {(min5 + 1u) >> 1,          (min5 + c[2] + 2u) >> 1, (c[2] + c[3] + 2u) >> 1,
+                           (c[3] + c[4] + 2u) >> 1,   (c[4] + c[5] + 2u) >> 1, (c[5] + max5 + 1u) >> 1,
+                           min((max5 + 257u) >> 1, 255u)};
+#pragma unroll
+    for (int j = 0; j < 7; ++j) bk.t[j] = t[j] * 0x01010101u;
+    bk.idx_lo = 6u | (0u << 8) | (2u << 16) | (3u << 24);
+    bk.idx_hi = 4u | (5u << 8) | (1u << 16) | ((max5 == 255u ? 1u : 7u) << 24);
+    bk.val_lo = (min5 << 8) | (c[2] << 16) | (c[3] << 24);
+    bk.val_hi = c[4] | (c[5] << 8) | (max5 << 16) | (255u << 24);
     return bk;
 }
 
@@ -376,8 +387,8 @@ __device__ __forceinline__ uint2 encode_bc3_alpha(const uint32_t (&v)[4], uint32
     for (int i = 1; i < 7; ++i) c7[1 + i] = (uint32_t)(((7 - i) * min7 + i * max7) / 7);
     uint32_t i5[4], i7[4];
     // errors compared without their common x^2 part
-    const int e5 = fit_book(v, vm, make_book<true>(c5), i5);
-    const int e7 = fit_book(v, vm, make_book<false>(c7), i7);
+    const int e5 = fit_book(v, vm, make_book5((uint32_t)min5, (uint32_t)max5, c5), i5);
+    const int e7 = fit_book(v, vm, make_book(c7), i7);
     uint32_t out[4];
     if (e5 <= e7) {
         // write_alpha_block5: a0 > a1 cannot occur after fix_range; kept for fidelity
