@@ -8,13 +8,15 @@
 //               every 32nd block of it;
 //   team units  ClusterFit, IterativeClusterFit -- a team of 32 lanes encodes
 //               the unit's C blocks one after another.
-// Each queue is drained by a persistent kernel (grid = SMs x CTAs per SM);
-// warps pop units with one atomicAdd on the queue's counter, so uneven levels
+// Each queue is drained by persistent kernels (grid = SMs x CTAs per SM);
+// warps pop units with one atomicAdd on a queue counter, so uneven levels
 // (4x4 mips next to 4096x4096 bases) balance themselves.  Team units are
-// ordered most expensive first (iterative before single-pass).  The two
+// grouped by class (format x iterative or single-pass), iterative classes
+// first, and each class is drained by its own kernel instantiation, so each
+// gets the register budget its code needs.  The lane kernel and the team
 // kernels run on two streams forked from the caller's stream; a launch is a
-// memset of the counters plus the two kernels, so it can be captured in a
-// CUDA graph and replayed.
+// memset of the counters plus the kernels, so it can be captured in a CUDA
+// graph and replayed.
 //
 // The per-block code is the single-texture code (tx_colour.cuh,
 // tx_alpha.cuh), so a batch produces exactly the bytes of per-texture calls.
@@ -37,8 +39,9 @@ namespace tx {
 
 cudaError_t upload_batch_tables(const uint32_t lut[4][256][2]) { return upload_tables_this_tu(lut); }
 
-template <int TEAM>
-__global__ void __launch_bounds__(256, 3) k_batch_teams(BatchQueue q) {
+// One team class: every unit of q is (FMT, NITER).
+template <int TEAM, int FMT, int NITER>
+__global__ void __launch_bounds__(256, 4) k_batch_teams(BatchQueue q) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ float s_unorm[256];
     __shared__ float s_sqrt[17];
@@ -47,29 +50,51 @@ __global__ void __launch_bounds__(256, 3) k_batch_teams(BatchQueue q) {
     const TeamTables tt{g_cand, g_cand + kCand4 + 1, s_unorm, s_sqrt};
     const Team<TEAM> tm;
     TeamSmem &sm = teams[threadIdx.x / TEAM];
-    for (;;) {
+    if (NITER == 1) {
+        for (;;) {
+            uint32_t u = 0;
+            if (tm.lane == 0) u = atomicAdd(q.counter, 1u);
+            u = tm.shfl(u, 0);
+            if (u >= q.nunits) break;
+            const uint2 unit = q.units[u];
+            const BatchItem &it = q.items[unit.x];
+            const SrcDesc src = it.src;
+            const DevParams prm = it.prm;
+            uint8_t *dst = it.dst;
+            const uint32_t end = min(unit.y + q.per_unit, it.nblocks);
+            for (uint32_t b = unit.y; b < end; ++b) cluster_block<FMT, TEAM, NITER>(tm, sm, tt, src, b, prm, dst);
+        }
+        return;
+    }
+    // IterativeClusterFit: a block takes long enough that the queue pop and
+    // the pixel loads of the next block are issued before the current block
+    // is encoded, so their latency hides behind it.
+    auto pop = [&](uint32_t &item, uint32_t &b, uint32_t &end) {
         uint32_t u = 0;
         if (tm.lane == 0) u = atomicAdd(q.counter, 1u);
         u = tm.shfl(u, 0);
-        if (u >= q.nunits) break;
+        if (u >= q.nunits) return false;
         const uint2 unit = q.units[u];
-        const BatchItem &it = q.items[unit.x];
-        const SrcDesc src = it.src;
-        const DevParams prm = it.prm;
-        uint8_t *dst = it.dst;
-        const uint32_t end = min(unit.y + q.per_unit, it.nblocks);
-        const int sel = it.format * 2 + (it.kind == KIND_CLUSTER_ITER ? 1 : 0);
-        for (uint32_t b = unit.y; b < end; ++b) {
-            switch (sel) {
-            case BC1 * 2: cluster_block<BC1, TEAM, 1>(tm, sm, tt, src, b, prm, dst); break;
-            case BC1 * 2 + 1: cluster_block<BC1, TEAM, 8>(tm, sm, tt, src, b, prm, dst); break;
-            case BC2 * 2: cluster_block<BC2, TEAM, 1>(tm, sm, tt, src, b, prm, dst); break;
-            case BC2 * 2 + 1: cluster_block<BC2, TEAM, 8>(tm, sm, tt, src, b, prm, dst); break;
-            case BC3 * 2: cluster_block<BC3, TEAM, 1>(tm, sm, tt, src, b, prm, dst); break;
-            case BC3 * 2 + 1: cluster_block<BC3, TEAM, 8>(tm, sm, tt, src, b, prm, dst); break;
-            default: break;
-            }
-        }
+        item = unit.x;
+        b = unit.y;
+        end = min(unit.y + q.per_unit, q.items[unit.x].nblocks);
+        return true;
+    };
+    uint32_t ci, cb, ce;
+    if (!pop(ci, cb, ce)) return;
+    TeamPixel tp = load_team_pixel(q.items[ci].src, cb, tm.lane);
+    for (;;) {
+        uint32_t ni = ci, nb = cb + 1, ne = ce;
+        const bool more = nb < ne || pop(ni, nb, ne);
+        TeamPixel tn{0u, false};
+        if (more) tn = load_team_pixel(q.items[ni].src, nb, tm.lane);
+        const BatchItem &it = q.items[ci];
+        cluster_block_px<FMT, TEAM, NITER>(tm, sm, tt, tp, cb, it.prm, it.dst);
+        if (!more) break;
+        ci = ni;
+        cb = nb;
+        ce = ne;
+        tp = tn;
     }
 }
 
@@ -157,8 +182,9 @@ struct tx_batch {
     std::vector<tx::BatchItem> desc;
     tx::BatchItem *d_items = nullptr;
     uint2 *d_lane_units = nullptr, *d_team_units = nullptr;
-    uint32_t *d_counters = nullptr;
+    uint32_t *d_counters = nullptr;  // lane queue, then one per team class
     uint32_t n_lane = 0, n_team = 0;
+    uint32_t team_counts[tx::kTeamClasses] = {};
     size_t nblocks = 0;
     tx_batch_tuning tuning{};
     cudaStream_t side = nullptr;
@@ -168,7 +194,7 @@ struct tx_batch {
 
 namespace {
 
-constexpr int kTeamMaxThreads = 256;  // __launch_bounds__ of k_batch_teams
+constexpr int kTeamMaxThreads = 256;  // __launch_bounds__ of the k_batch_teams kernels
 
 void default_tuning(tx_batch_tuning *t) {
     t->team_lanes = 32;
@@ -199,7 +225,7 @@ int fail_batch(cudaError_t e) {
 
 // (Re)build the unit queues for the current tuning and upload them.
 int build_units(tx_batch *b) {
-    std::vector<uint2> lane, team_iter, team;
+    std::vector<uint2> lane, cls[tx::kTeamClasses], team_iter;
     const uint32_t lane_span = 32u * (uint32_t)b->tuning.lane_blocks_per_lane;
     const uint32_t team_span = (uint32_t)b->tuning.team_blocks_per_unit;
     for (uint32_t i = 0; i < b->desc.size(); ++i) {
@@ -207,11 +233,14 @@ int build_units(tx_batch *b) {
         if (d.kind == tx::KIND_ALPHA || d.kind == tx::KIND_RANGE) {
             for (uint32_t f = 0; f < d.nblocks; f += lane_span) lane.push_back(make_uint2(i, f));
         } else {
-            auto &dst = d.kind == tx::KIND_CLUSTER_ITER ? team_iter : team;
+            auto &dst = cls[tx::team_class(d.format, d.kind)];
             for (uint32_t f = 0; f < d.nblocks; f += team_span) dst.push_back(make_uint2(i, f));
         }
     }
-    team_iter.insert(team_iter.end(), team.begin(), team.end());  // most expensive first
+    for (int c = 0; c < tx::kTeamClasses; ++c) {  // class order: iterative (most expensive) first
+        b->team_counts[c] = (uint32_t)cls[c].size();
+        team_iter.insert(team_iter.end(), cls[c].begin(), cls[c].end());
+    }
     cudaFree(b->d_lane_units);
     cudaFree(b->d_team_units);
     b->d_lane_units = b->d_team_units = nullptr;
@@ -232,29 +261,6 @@ int build_units(tx_batch *b) {
     return TX_OK;
 }
 
-template <int TEAM>
-cudaError_t launch_teams(tx_batch *b, cudaStream_t st) {
-    const int threads = b->tuning.team_threads_per_cta;
-    const size_t smem = tx::cluster_smem_bytes(TEAM, threads);
-    static bool attr_set[64][2] = {};
-    if (b->device < 64 && !attr_set[b->device][TEAM == 16]) {
-        cudaError_t e = cudaFuncSetAttribute(tx::k_batch_teams<TEAM>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)tx::cluster_smem_bytes(TEAM, 256));
-        if (e != cudaSuccess) return e;
-        attr_set[b->device][TEAM == 16] = true;
-    }
-    const uint32_t units_per_cta = (uint32_t)(threads / TEAM);
-    uint32_t grid = (uint32_t)(b->sm_count * b->tuning.team_ctas_per_sm);
-    const uint32_t need = (b->n_team + units_per_cta - 1) / units_per_cta;
-    if (grid > need) grid = need;
-    if (grid == 0) grid = 1;
-    tx::BatchQueue q{b->d_items, b->d_team_units, b->n_team, b->d_counters + 1,
-                     (uint32_t)b->tuning.team_blocks_per_unit};
-    tx::k_batch_teams<TEAM><<<grid, threads, smem, st>>>(q);
-    tx::note_launch();
-    return cudaGetLastError();
-}
-
 cudaError_t launch_lanes(tx_batch *b, cudaStream_t st) {
     uint32_t grid = (uint32_t)(b->sm_count * b->tuning.lane_ctas_per_sm);
     const uint32_t need = (b->n_lane + 3) / 4;  // 4 warps per CTA
@@ -269,14 +275,17 @@ cudaError_t launch_lanes(tx_batch *b, cudaStream_t st) {
 
 int launch_impl(tx_batch *b, cudaStream_t st) {
     cudaError_t e;
-    if ((e = cudaMemsetAsync(b->d_counters, 0, 2 * sizeof(uint32_t), st)) != cudaSuccess) return fail_batch(e);
+    if ((e = cudaMemsetAsync(b->d_counters, 0, tx::kBatchCounters * sizeof(uint32_t), st)) != cudaSuccess)
+        return fail_batch(e);
     const bool both = b->n_lane && b->n_team;
     if (both) {
         if ((e = cudaEventRecord(b->fork, st)) != cudaSuccess) return fail_batch(e);
         if ((e = cudaStreamWaitEvent(b->side, b->fork, 0)) != cudaSuccess) return fail_batch(e);
     }
     if (b->n_team) {
-        e = b->tuning.team_lanes == 16 ? launch_teams<16>(b, st) : launch_teams<32>(b, st);
+        e = tx::launch_team_classes(b->d_items, b->d_team_units, b->team_counts,
+                                    (uint32_t)b->tuning.team_blocks_per_unit, b->d_counters + 1, b->sm_count,
+                                    b->tuning, st);
         if (e != cudaSuccess) return fail_batch(e);
     }
     if (b->n_lane) {
@@ -409,7 +418,10 @@ int tx_batch_create(const tx_batch_item *items, size_t nitems, const tx_batch_tu
             return fail_batch(e);
         }
     }
-    if ((e = cudaMalloc(&b->d_counters, 2 * sizeof(uint32_t))) != cudaSuccess) { tx_batch_destroy(b); return fail_batch(e); }
+    if ((e = cudaMalloc(&b->d_counters, tx::kBatchCounters * sizeof(uint32_t))) != cudaSuccess) {
+        tx_batch_destroy(b);
+        return fail_batch(e);
+    }
     if ((e = cudaStreamCreateWithFlags(&b->side, cudaStreamNonBlocking)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming)) != cudaSuccess ||
         (e = cudaEventCreateWithFlags(&b->join, cudaEventDisableTiming)) != cudaSuccess) {
@@ -550,7 +562,7 @@ namespace tx {
 
 constexpr size_t kNoallocScratchBytes = (size_t)1 << 20;  // 1 MiB per device
 constexpr uint32_t kNoallocMaxItems = 256;                // texture levels per call
-constexpr size_t kNoallocItemsOff = 256;                  // after the two counters
+constexpr size_t kNoallocItemsOff = 256;                  // after the queue counters
 constexpr size_t kNoallocUnitsOff =
     (kNoallocItemsOff + kNoallocMaxItems * sizeof(BatchItem) + 255) & ~(size_t)255;
 constexpr uint32_t kNoallocMaxUnits = (uint32_t)((kNoallocScratchBytes - kNoallocUnitsOff) / sizeof(uint2));
@@ -565,14 +577,15 @@ struct NoallocSetup {
 };
 
 // One CTA: copy the item table into the scratch array, clear the counters and
-// write both unit queues (lane units first, then team units in item order).
+// write both unit queues (lane units first, then team units in item order,
+// which the host has grouped by team class).
 __global__ void __launch_bounds__(kNoallocMaxItems) k_noalloc_setup(const __grid_constant__ NoallocSetup p) {
     uint32_t *counters = reinterpret_cast<uint32_t *>(g_noalloc_scratch);
     BatchItem *items = reinterpret_cast<BatchItem *>(g_noalloc_scratch + kNoallocItemsOff);
     uint2 *units = reinterpret_cast<uint2 *>(g_noalloc_scratch + kNoallocUnitsOff);
     __shared__ uint32_t sl[kNoallocMaxItems], stm[kNoallocMaxItems];
     const uint32_t t = threadIdx.x;
-    if (t < 2) counters[t] = 0;
+    if (t < (uint32_t)kBatchCounters) counters[t] = 0;
     uint32_t nl = 0, nt = 0;
     if (t < p.nitems) {
         const BatchItem &it = p.items[t];
@@ -620,9 +633,7 @@ int noalloc_setup_device(int dev, NoallocDevice **out) {
         if (e != cudaSuccess) return fail_batch(e);
         if ((e = cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
             return fail_batch(e);
-        if ((e = cudaFuncSetAttribute(tx::k_batch_teams<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                      (int)tx::cluster_smem_bytes(32, 256))) != cudaSuccess)
-            return fail_batch(e);
+        if ((e = tx::prepare_team_kernels()) != cudaSuccess) return fail_batch(e);
         d.scratch = static_cast<unsigned char *>(ptr);
         d.ready = true;
     }
@@ -638,11 +649,10 @@ extern "C" int tx_batch_launch_noalloc(const tx_batch_item *items, size_t nitems
     static_assert(sizeof(tx::NoallocSetup) <= 32000, "kernel parameter block too large");
     tx::NoallocSetup setup;
     std::memset(&setup, 0, sizeof(setup));
-    // order: lane items and iterative ClusterFit items first, so the team
-    // queue starts with its most expensive units
+    // order: lane items first, then the ClusterFit items by team class
+    // (iterative first), so the team queue comes out grouped by class
     uint32_t n = 0;
-    uint64_t lane_blocks = 0, team_blocks = 0;
-    for (int pass = 0; pass < 2; ++pass) {
+    for (int pass = 0; pass <= tx::kTeamClasses; ++pass) {
         for (size_t i = 0; i < nitems; ++i) {
             const tx_batch_item &it = items[i];
             const size_t bs = tx_block_size(it.format);
@@ -657,8 +667,9 @@ extern "C" int tx_batch_launch_noalloc(const tx_batch_item *items, size_t nitems
             const size_t nb = tx_num_blocks(it.width) * tx_num_blocks(it.height);
             if (nb > 0xFFFFFFF0u) return TX_ERR_INVALID_ARGUMENT;
             const bool lane = it.format == TX_FORMAT_BC4 || it.format == TX_FORMAT_BC5 || alg == TX_RANGE_FIT;
-            const bool first = lane || alg == TX_ITERATIVE_CLUSTER_FIT;
-            if (first != (pass == 0)) continue;
+            const int kind = lane ? (alg == TX_RANGE_FIT && it.format <= TX_FORMAT_BC3 ? tx::KIND_RANGE : tx::KIND_ALPHA)
+                                  : (alg == TX_ITERATIVE_CLUSTER_FIT ? tx::KIND_CLUSTER_ITER : tx::KIND_CLUSTER);
+            if (pass != (lane ? 0 : 1 + tx::team_class(it.format, kind))) continue;
             tx::BatchItem &d = setup.items[n++];
             d.src.base = static_cast<const uint8_t *>(it.src);
             d.src.masks = nullptr;
@@ -676,20 +687,25 @@ extern "C" int tx_batch_launch_noalloc(const tx_batch_item *items, size_t nitems
             d.nblocks = (uint32_t)nb;
             d.format = it.format;
             d.channels = it.channels;
-            d.kind = lane ? (alg == TX_RANGE_FIT && it.format <= TX_FORMAT_BC3 ? tx::KIND_RANGE : tx::KIND_ALPHA)
-                          : (alg == TX_ITERATIVE_CLUSTER_FIT ? tx::KIND_CLUSTER_ITER : tx::KIND_CLUSTER);
-            (lane ? lane_blocks : team_blocks) += nb;
+            d.kind = kind;
         }
     }
     setup.nitems = n;
     // unit sizes: the defaults, doubled until both queues fit the scratch array
     uint32_t lane_span = 64, team_span = 1;
+    uint32_t team_counts[tx::kTeamClasses] = {};
     auto count_units = [&](uint64_t *nl, uint64_t *nt) {
         *nl = *nt = 0;
+        for (int c = 0; c < tx::kTeamClasses; ++c) team_counts[c] = 0;
         for (uint32_t i = 0; i < n; ++i) {
             const tx::BatchItem &d = setup.items[i];
-            if (d.kind == tx::KIND_ALPHA || d.kind == tx::KIND_RANGE) *nl += (d.nblocks + lane_span - 1) / lane_span;
-            else *nt += (d.nblocks + team_span - 1) / team_span;
+            if (d.kind == tx::KIND_ALPHA || d.kind == tx::KIND_RANGE) {
+                *nl += (d.nblocks + lane_span - 1) / lane_span;
+            } else {
+                const uint32_t u = (d.nblocks + team_span - 1) / team_span;
+                *nt += u;
+                team_counts[tx::team_class(d.format, d.kind)] += u;
+            }
         }
     };
     uint64_t n_lane = 0, n_team = 0;
@@ -701,8 +717,6 @@ extern "C" int tx_batch_launch_noalloc(const tx_batch_item *items, size_t nitems
     }
     setup.lane_span = lane_span;
     setup.team_span = team_span;
-    (void)lane_blocks;
-    (void)team_blocks;
 
     int rc = tx_internal_ensure_device();
     if (rc != TX_OK) return rc;
@@ -729,12 +743,11 @@ extern "C" int tx_batch_launch_noalloc(const tx_batch_item *items, size_t nitems
         if ((e = cudaGetLastError()) != cudaSuccess) return fail_batch(e);
     }
     if (n_team) {
-        tx::BatchQueue q{d_items, d_units + n_lane, (uint32_t)n_team, d_counters + 1, team_span};
-        uint32_t grid = (uint32_t)(nd->sm_count * 3);
-        grid = std::min<uint32_t>(grid, (uint32_t)((n_team + 7) / 8));
-        tx::k_batch_teams<32><<<grid, 256, tx::cluster_smem_bytes(32, 256), st>>>(q);
-        tx::note_launch();
-        if ((e = cudaGetLastError()) != cudaSuccess) return fail_batch(e);
+        tx_batch_tuning t;
+        default_tuning(&t);
+        if ((e = tx::launch_team_classes(d_items, d_units + n_lane, team_counts, team_span, d_counters + 1,
+                                         nd->sm_count, t, st)) != cudaSuccess)
+            return fail_batch(e);
     }
     return TX_OK;
 }
@@ -766,10 +779,79 @@ void fill_batch_item(const tx_batch_item &it, BatchItem *d) {
     else d->kind = alg == TX_ITERATIVE_CLUSTER_FIT ? KIND_CLUSTER_ITER : KIND_CLUSTER;
 }
 
+// The team kernels need more than 48 KB of dynamic shared memory: raise the
+// limit once per device and kernel.
+template <int TEAM, int FMT, int NITER>
+static cudaError_t class_attr() {
+    static bool attr_set[64] = {};
+    int dev = 0;
+    cudaGetDevice(&dev);
+    if (dev < 64 && !attr_set[dev]) {
+        const cudaError_t e = cudaFuncSetAttribute(k_batch_teams<TEAM, FMT, NITER>,
+                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                                   (int)cluster_smem_bytes(TEAM, 256));
+        if (e != cudaSuccess) return e;
+        attr_set[dev] = true;
+    }
+    return cudaSuccess;
+}
+
+cudaError_t prepare_team_kernels() {
+    cudaError_t e;
+    if ((e = class_attr<32, BC1, 8>()) != cudaSuccess || (e = class_attr<32, BC2, 8>()) != cudaSuccess ||
+        (e = class_attr<32, BC3, 8>()) != cudaSuccess || (e = class_attr<32, BC1, 1>()) != cudaSuccess ||
+        (e = class_attr<32, BC2, 1>()) != cudaSuccess || (e = class_attr<32, BC3, 1>()) != cudaSuccess)
+        return e;
+    return cudaSuccess;
+}
+
+template <int TEAM, int FMT, int NITER>
+static cudaError_t launch_one_class(const BatchQueue &q, uint32_t grid, int threads, cudaStream_t st) {
+    const cudaError_t e = class_attr<TEAM, FMT, NITER>();
+    if (e != cudaSuccess) return e;
+    k_batch_teams<TEAM, FMT, NITER><<<grid, threads, cluster_smem_bytes(TEAM, threads), st>>>(q);
+    note_launch();
+    return cudaGetLastError();
+}
+
+template <int TEAM>
+static cudaError_t launch_class(int c, const BatchQueue &q, uint32_t grid, int threads, cudaStream_t st) {
+    switch (c) {
+    case 0: return launch_one_class<TEAM, BC1, 8>(q, grid, threads, st);
+    case 1: return launch_one_class<TEAM, BC2, 8>(q, grid, threads, st);
+    case 2: return launch_one_class<TEAM, BC3, 8>(q, grid, threads, st);
+    case 3: return launch_one_class<TEAM, BC1, 1>(q, grid, threads, st);
+    case 4: return launch_one_class<TEAM, BC2, 1>(q, grid, threads, st);
+    case 5: return launch_one_class<TEAM, BC3, 1>(q, grid, threads, st);
+    default: return cudaErrorInvalidValue;
+    }
+}
+
+cudaError_t launch_team_classes(const BatchItem *d_items, const uint2 *d_team,
+                                const uint32_t (&team_counts)[kTeamClasses], uint32_t team_blocks_per_unit,
+                                uint32_t *counters, int sm_count, const tx_batch_tuning &t, cudaStream_t st) {
+    const int threads = t.team_threads_per_cta;
+    const int team = t.team_lanes == 16 ? 16 : 32;
+    const uint32_t per = (uint32_t)(threads / team);
+    uint32_t begin = 0;
+    for (int c = 0; c < kTeamClasses; ++c) {
+        const uint32_t n = team_counts[c];
+        if (n == 0) continue;
+        uint32_t grid = (uint32_t)(sm_count * t.team_ctas_per_sm);
+        grid = std::max<uint32_t>(1, std::min<uint32_t>(grid, (n + per - 1) / per));
+        const BatchQueue q{d_items, d_team + begin, n, counters + c, team_blocks_per_unit};
+        begin += n;
+        const cudaError_t e = team == 16 ? launch_class<16>(c, q, grid, threads, st)
+                                         : launch_class<32>(c, q, grid, threads, st);
+        if (e != cudaSuccess) return e;
+    }
+    return cudaSuccess;
+}
+
 cudaError_t launch_batch_queues(const BatchItem *d_items, const uint2 *d_lane, uint32_t n_lane,
-                                uint32_t lane_blocks_per_lane, const uint2 *d_team, uint32_t n_team,
-                                uint32_t team_blocks_per_unit, uint32_t *d_counters, int sm_count,
-                                const tx_batch_tuning &t, cudaStream_t st) {
+                                uint32_t lane_blocks_per_lane, const uint2 *d_team,
+                                const uint32_t (&team_counts)[kTeamClasses], uint32_t team_blocks_per_unit,
+                                uint32_t *d_counters, int sm_count, const tx_batch_tuning &t, cudaStream_t st) {
     if (n_lane) {
         uint32_t grid = (uint32_t)(sm_count * t.lane_ctas_per_sm);
         grid = std::max<uint32_t>(1, std::min<uint32_t>(grid, (n_lane + 3) / 4));
@@ -779,29 +861,7 @@ cudaError_t launch_batch_queues(const BatchItem *d_items, const uint2 *d_lane, u
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return e;
     }
-    if (n_team) {
-        const int threads = t.team_threads_per_cta;
-        const int team = t.team_lanes == 16 ? 16 : 32;
-        uint32_t grid = (uint32_t)(sm_count * t.team_ctas_per_sm);
-        const uint32_t per = (uint32_t)(threads / team);
-        grid = std::max<uint32_t>(1, std::min<uint32_t>(grid, (n_team + per - 1) / per));
-        BatchQueue q{d_items, d_team, n_team, d_counters + 1, team_blocks_per_unit};
-        cudaError_t e;
-        if (team == 16) {
-            e = cudaFuncSetAttribute(k_batch_teams<16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)cluster_smem_bytes(16, 256));
-            if (e != cudaSuccess) return e;
-            k_batch_teams<16><<<grid, threads, cluster_smem_bytes(16, threads), st>>>(q);
-        } else {
-            e = cudaFuncSetAttribute(k_batch_teams<32>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)cluster_smem_bytes(32, 256));
-            if (e != cudaSuccess) return e;
-            k_batch_teams<32><<<grid, threads, cluster_smem_bytes(32, threads), st>>>(q);
-        }
-        note_launch();
-        if ((e = cudaGetLastError()) != cudaSuccess) return e;
-    }
-    return cudaSuccess;
+    return launch_team_classes(d_items, d_team, team_counts, team_blocks_per_unit, d_counters + 1, sm_count, t, st);
 }
 
 }  // namespace tx

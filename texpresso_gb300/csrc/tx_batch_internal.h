@@ -26,14 +26,37 @@ struct BatchQueue {
     uint32_t per_unit;      // lane units: blocks per lane; team units: blocks per unit
 };
 
+// Team units are grouped by class, each drained by its own kernel
+// instantiation (so each gets the registers its code needs): class =
+// (iterative ? 0 : 3) + format (BC1, BC2, BC3), iterative classes first.
+constexpr int kTeamClasses = 6;
+constexpr int kBatchCounters = 1 + kTeamClasses;  // lane queue, then one per team class
+
+__host__ __device__ inline int team_class(int format, int kind) {
+    return (kind == KIND_CLUSTER_ITER ? 0 : 3) + format;
+}
+
 // Fill a device descriptor from a validated public item.
 void fill_batch_item(const tx_batch_item &it, BatchItem *d);
 
-// Enqueue the two persistent kernels over device-resident queues on `st`
-// (sequentially).  counters[0..1] must be zero when the kernels start.
+// Enqueue the persistent kernels of one team queue whose units are grouped by
+// class (team_counts[c] units of class c, in class order) on `st`, one kernel
+// per non-empty class, one after another.  counters[c] belongs to class c and
+// must be zero when its kernel starts.
+cudaError_t launch_team_classes(const BatchItem *d_items, const uint2 *d_team,
+                                const uint32_t (&team_counts)[kTeamClasses], uint32_t team_blocks_per_unit,
+                                uint32_t *counters, int sm_count, const tx_batch_tuning &tuning, cudaStream_t st);
+
+// Raise the shared-memory limit of every team kernel with 32-lane teams on
+// the current device (done by a plain launch on first use otherwise).
+cudaError_t prepare_team_kernels();
+
+// Enqueue the lane kernel and the team kernels over device-resident queues on
+// `st` (sequentially).  counters[0 .. kBatchCounters) must be zero when the
+// kernels start.
 cudaError_t launch_batch_queues(const BatchItem *d_items, const uint2 *d_lane, uint32_t n_lane,
-                                uint32_t lane_blocks_per_lane, const uint2 *d_team, uint32_t n_team,
-                                uint32_t team_blocks_per_unit, uint32_t *d_counters, int sm_count,
-                                const tx_batch_tuning &tuning, cudaStream_t st);
+                                uint32_t lane_blocks_per_lane, const uint2 *d_team,
+                                const uint32_t (&team_counts)[kTeamClasses], uint32_t team_blocks_per_unit,
+                                uint32_t *d_counters, int sm_count, const tx_batch_tuning &tuning, cudaStream_t st);
 
 }  // namespace tx

@@ -251,8 +251,8 @@ int schedule_step(tx_server *s) {
     if (ready.empty()) return TX_OK;
     const uint32_t cap = s->cfg.step_blocks;
     const size_t share = std::max<size_t>(s->cfg.min_share, cap / ready.size());
-    uint32_t n_items = 0, n_lane = 0, n_team_iter = 0, n_team = 0;
-    std::vector<uint2> lane_units, iter_units, team_units;
+    uint32_t n_items = 0, n_lane = 0;
+    std::vector<uint2> lane_units, class_units[tx::kTeamClasses];
     const uint32_t lane_span = 32u * (uint32_t)s->cfg.tuning.lane_blocks_per_lane;
     const uint32_t team_span = (uint32_t)s->cfg.tuning.team_blocks_per_unit;
     size_t budget = cap;
@@ -279,7 +279,7 @@ int schedule_step(tx_server *s) {
             const tx::BatchItem &d = st.h_items[n_items];
             const bool lane = d.kind == tx::KIND_ALPHA || d.kind == tx::KIND_RANGE;
             const uint32_t span = lane ? lane_span : team_span;
-            auto &dst = lane ? lane_units : (d.kind == tx::KIND_CLUSTER_ITER ? iter_units : team_units);
+            auto &dst = lane ? lane_units : class_units[tx::team_class(d.format, d.kind)];
             for (uint32_t f = nb; f < nb + n; f += span) dst.push_back(make_uint2(n_items, f));
             // a unit may run past this step's share; the kernels stop at the level's end,
             // so round the share up to whole units
@@ -295,13 +295,16 @@ int schedule_step(tx_server *s) {
     }
     s->rr = start + 1;
     n_lane = (uint32_t)lane_units.size();
-    n_team_iter = (uint32_t)iter_units.size();
-    n_team = (uint32_t)team_units.size();
-    const uint32_t total = n_lane + n_team_iter + n_team;
+    uint32_t team_counts[tx::kTeamClasses];
+    uint32_t total = n_lane;
+    for (int c = 0; c < tx::kTeamClasses; ++c) {
+        team_counts[c] = (uint32_t)class_units[c].size();
+        total += team_counts[c];
+    }
     if (total > s->max_units) return TX_ERR_INVALID_ARGUMENT;  // cannot happen: units <= step_blocks + items
     std::memcpy(st.h_units, lane_units.data(), n_lane * sizeof(uint2));
-    std::memcpy(st.h_units + n_lane, iter_units.data(), n_team_iter * sizeof(uint2));
-    std::memcpy(st.h_units + n_lane + n_team_iter, team_units.data(), n_team * sizeof(uint2));
+    for (uint32_t c = 0, off = n_lane; c < (uint32_t)tx::kTeamClasses; off += team_counts[c], ++c)
+        std::memcpy(st.h_units + off, class_units[c].data(), team_counts[c] * sizeof(uint2));
     cudaError_t e;
     nvtxRangePushA("tx_server step");
     if ((e = cudaMemcpyAsync(st.d_items, st.h_items, n_items * sizeof(tx::BatchItem), cudaMemcpyHostToDevice,
@@ -310,9 +313,9 @@ int schedule_step(tx_server *s) {
     if ((e = cudaMemcpyAsync(st.d_units, st.h_units, total * sizeof(uint2), cudaMemcpyHostToDevice, s->s_comp)) !=
         cudaSuccess)
         return fail_server(e);
-    if ((e = cudaMemsetAsync(st.d_counters, 0, 2 * sizeof(uint32_t), s->s_comp)) != cudaSuccess) return fail_server(e);
+    if ((e = cudaMemsetAsync(st.d_counters, 0, tx::kBatchCounters * sizeof(uint32_t), s->s_comp)) != cudaSuccess) return fail_server(e);
     if ((e = tx::launch_batch_queues(st.d_items, st.d_units, n_lane, lane_span / 32, st.d_units + n_lane,
-                                     n_team_iter + n_team, team_span, st.d_counters, s->sm_count, s->cfg.tuning,
+                                     team_counts, team_span, st.d_counters, s->sm_count, s->cfg.tuning,
                                      s->s_comp)) != cudaSuccess)
         return fail_server(e);
     if ((e = cudaEventRecord(st.done, s->s_comp)) != cudaSuccess) return fail_server(e);
@@ -510,7 +513,7 @@ int tx_server_create(const tx_server_config *config, tx_server **out) {
     for (Step &st : s->steps) {
         if (e == cudaSuccess) e = cudaMalloc(&st.d_items, s->max_items * sizeof(tx::BatchItem));
         if (e == cudaSuccess) e = cudaMalloc(&st.d_units, s->max_units * sizeof(uint2));
-        if (e == cudaSuccess) e = cudaMalloc(&st.d_counters, 2 * sizeof(uint32_t));
+        if (e == cudaSuccess) e = cudaMalloc(&st.d_counters, tx::kBatchCounters * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMallocHost(&st.h_items, s->max_items * sizeof(tx::BatchItem));
         if (e == cudaSuccess) e = cudaMallocHost(&st.h_units, s->max_units * sizeof(uint2));
         if (e == cudaSuccess) e = cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming);
