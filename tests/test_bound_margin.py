@@ -1,5 +1,6 @@
-"""The ClusterFit pruning bound (cand_bound / lb_terms in
-texpresso_gb300/csrc/tx_colour.cuh), restated in numpy, never exceeds the
+"""The ClusterFit pruning bounds (cand_bound / lb_terms, and unit_bound /
+unit_terms for 16 colours of weight 1, in texpresso_gb300/csrc/tx_colour.cuh),
+restated in numpy, never exceeds the
 reference's error (the numpy oracle's f32 evaluation) on any candidate of
 natural, palette and 5:6:5-grid blocks under several weight sets, with and
 without alpha weighting.  FMA steps are emulated in double and rounded once,
@@ -60,6 +61,52 @@ def bounds(P0, P1, P2, xs, w, nc):
     return lbm, lb0, margin
 
 
+def wterms(P0w, P1w, P2w, xsw, nc):
+    """The reference's f32 alpha2, beta2, alphabeta (wterms4 / wterms3)."""
+    if nc == 4:
+        p3w = (((xsw - P2w).astype(f32) - P1w).astype(f32) - P0w).astype(f32)
+        al = ((P2w * f32(1 / 9)).astype(f32) + ((P1w * f32(4 / 9)).astype(f32) + P0w).astype(f32)).astype(f32)
+        be = ((P1w * f32(1 / 9)).astype(f32) + ((P2w * f32(4 / 9)).astype(f32) + p3w).astype(f32)).astype(f32)
+        ab = (f32(2 / 9) * (P1w + P2w).astype(f32)).astype(f32)
+    else:
+        p2w = ((xsw - P1w).astype(f32) - P0w).astype(f32)
+        al = fma(P1w, f32(0.25), P0w)
+        be = fma(P1w, f32(0.25), p2w)
+        ab = (P1w * f32(0.25)).astype(f32)
+    return al, be, ab
+
+
+def unit_bounds(P0, P1, P2, xs, w, nc):
+    """unit_bound with the unit_terms table, as the kernel computes it for a
+    16-colour set of weight-1 points."""
+    al, be, ga = (v.astype(np.float64) for v in wterms(P0[:, 3], P1[:, 3], P2[:, 3], xs[3], nc))
+    det = al * be - ga * ga
+    A = al + be + 2 * ga
+    with np.errstate(all="ignore"):
+        F1 = np.where(det > 0, -A / det, np.nan).astype(f32)
+        r = np.where(det > 0, 2 * (al + ga) / A, 0).astype(f32)
+        C = np.where(det > 0, -(al + 2.0 ** -13) / det, np.nan).astype(f32)
+        C0 = np.where(det > 0, -al / det, np.nan).astype(f32)
+        f = np.where(det > 0, 1 / det, np.nan).astype(f32)
+        if nc == 4:
+            ax = fma(P2[:, :3], f32(1 / 3), fma(P1[:, :3], f32(2 / 3), P0[:, :3]))
+        else:
+            ax = fma(P1[:, :3], f32(0.5), P0[:, :3])
+        d = fma(-r[:, None], xs[None, :3], ax)
+        cwax = (w * ax).astype(f32)
+        sm = (cwax[:, 0] * d[:, 0]).astype(f32)
+        sm = fma(cwax[:, 1], d[:, 1], sm)
+        sm = fma(cwax[:, 2], d[:, 2], sm)
+        Z = f32(0)
+        for c in range(3):
+            Z = fma(w[c], (xs[c] * xs[c]).astype(f32), Z)
+        eps1 = f32(2.0 ** -17) * xs[3] * f32(w.sum())
+        lbm = fma(F1, sm, fma(C, Z, -eps1))
+        lb0 = fma(F1, sm, (C0 * Z).astype(f32))
+        margin = (f * (f32(2.0 ** -17) * xs[3] * Z) + eps1).astype(f32)
+    return lbm, lb0, margin
+
+
 def blocks():
     img = workloads.ramp_texture(64, 64, seed=9, alpha="ramp")
     nat = workloads.image_to_blocks(img)[0]
@@ -67,7 +114,7 @@ def blocks():
 
 
 def test_bound_never_exceeds_reference_error():
-    total, worst = 0, np.inf
+    total, worst, n_unit = 0, np.inf, 0
     for bi, blk in enumerate(blocks()):
         w = [np.array([0.2126, 0.7152, 0.0722], f32), np.array([1, 1, 1], f32),
              np.array([0.0, 1.0, 0.001], f32)][bi % 3]
@@ -91,13 +138,18 @@ def test_bound_never_exceeds_reference_error():
             P0, P1 = S[0, I], S[I, J]
             P2 = S[J, K] if nc == 4 else np.zeros_like(P0)
             err, _, _ = po._fit_all(P0, P1, P2 if nc == 4 else None, xs, w, nc)
-            lbm, lb0, margin = bounds(P0, P1, P2, xs, w, nc)
-            ok = np.isfinite(lbm)
-            assert np.all(err[ok] >= lbm[ok]), (bi, nc)
-            total += int(ok.sum())
-            if ok.any():
-                worst = min(worst, float(np.min((err[ok] - lb0[ok]) / margin[ok])))
+            forms = [bounds(P0, P1, P2, xs, w, nc)]
+            if n == 16 and np.all(wts == 1):
+                forms.append(unit_bounds(P0, P1, P2, xs, w, nc))
+                n_unit += 1
+            for lbm, lb0, margin in forms:
+                ok = np.isfinite(lbm)
+                assert np.all(err[ok] >= lbm[ok]), (bi, nc)
+                total += int(ok.sum())
+                if ok.any():
+                    worst = min(worst, float(np.min((err[ok] - lb0[ok]) / margin[ok])))
     assert total > 100000
+    assert n_unit > 100
     # the unmargined bound may fall below the error by rounding, never by more
     # than a small part of the margin
     assert worst > -0.25, worst

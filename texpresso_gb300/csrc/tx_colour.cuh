@@ -41,12 +41,14 @@ static __constant__ uint32_t c_ncand3[17];
 // 16-colour sets: a round of consecutive candidates then mostly shares S(0,i)
 // and S(i,j) and reads S(j,k) at consecutive addresses.
 static __device__ uint32_t g_cand16[kCand4 + 1 + kCand3 + 1];
-// Lower-bound terms (A, -2B, alpha2, 1/det) of the g_cand16 candidates of a
+// Lower-bound terms (F1, r, C, S offsets) of the g_cand16 candidates of a
 // 16-colour set whose weights are all exactly 1 (the w lanes of the partial
 // sums are then the counts i, j-i, k-j), from the reference's f32 alpha2,
-// beta2, alphabeta (see bound_terms; NaN when det <= 0: no bound).
-static __device__ float4 g_lb4[kCand4 + 1];
-static __device__ float4 g_lb3[kCand3 + 1];
+// beta2, alphabeta (see unit_terms and unit_bound; F1 = C = NaN when
+// det <= 0: no bound).  The w lane holds the bits i | S(i,j) << 8 |
+// S(j,k) << 16 (table offsets, one byte each).
+static __device__ float4 g_ub4[kCand4 + 1];
+static __device__ float4 g_ub3[kCand3 + 1];
 
 // Partial-sum table S(a,b), 0 <= a <= b <= 16, stored as the upper triangle
 // row by row: S(a,b) at tri_idx(a,b) (153 entries).
@@ -604,6 +606,32 @@ __device__ __forceinline__ float cand_bound(const float4 p0, const float4 p1, co
     return __fmaf_rn(-lt.w, acc, -bb.eps1);  // NaN when there is no bound: the candidate is kept
 }
 
+// The same bound for a 16-colour set of weight-1 points (W = 16), with the
+// candidate's constants folded into q = (F1, r, C) = (-A f, 2B / A,
+// -f (alpha + 2^-13)) (double, rounded once): since
+//     -f (A s1 - 2B s2) = F1 sum_c w_c ax_c (ax_c - r X_c)
+// and -f (alpha Z + Kb) = C Z (Kb = 2^-17 W Z = 2^-13 Z), the bound is
+//     F1 sum_c w_c ax_c (ax_c - r X_c) + C Z - eps1.
+// Rounding: A = W exactly, 0 <= r <= 2, so each of the three products is at
+// most 2 w_c X_c^2 in size and the sum carries at most ~10 u Z; with the
+// rounding of F1, r, C and the two final FMAs that is <= ~17 u f W Z, inside
+// the 26 u f W Z budgeted for the general form above.
+template <int NC>
+__device__ __forceinline__ float unit_bound(const float4 p0, const float4 p1, const float4 p2, const float4 q,
+                                            const float4 xs, const float (&cw)[3], const BoundBlock &bb) {
+    const float pa[3] = {p0.x, p0.y, p0.z}, pb[3] = {p1.x, p1.y, p1.z}, pc[3] = {p2.x, p2.y, p2.z};
+    const float X[3] = {xs.x, xs.y, xs.z};
+    float sum = 0.0f;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        const float ax = (NC == 4) ? __fmaf_rn(pc[c], 1.0f / 3.0f, __fmaf_rn(pb[c], 2.0f / 3.0f, pa[c]))
+                                   : __fmaf_rn(pb[c], 0.5f, pa[c]);
+        const float d = __fmaf_rn(-q.y, X[c], ax);
+        sum = c == 0 ? (cw[0] * ax) * d : __fmaf_rn(cw[c] * ax, d, sum);
+    }
+    return __fmaf_rn(q.x, sum, __fmaf_rn(q.z, bb.z, -bb.eps1));  // NaN when there is no bound
+}
+
 // Per-lane best of the candidates a lane evaluated exactly: error, entry and
 // endpoints, compared lexicographically on (error, entry).
 struct LaneBest {
@@ -737,18 +765,31 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
         } else {
             // 1. a lower bound of every candidate's error (see cand_bound)
             const BoundBlock bb = bound_block(xs, cw);
-            const float4 *lbt = NC == 4 ? g_lb4 : g_lb3;
             float lmin = __int_as_float(0x7f800000);
             uint32_t tseed = 0xFFFFFFFFu;
-            for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
-                const uint32_t e = __ldg(tbl + t);
-                const float4 p0 = sm.S[e & 0xFu];
-                const float4 p1 = sm.S[(e >> 4) & 0xFFu];
-                const float4 p2 = (NC == 4) ? sm.S[(e >> 12) & 0xFFu] : make_float4(0.f, 0.f, 0.f, 0.f);
-                const float4 lt = unit16 ? __ldg(lbt + t) : lb_terms<NC>(p0.w, p1.w, p2.w, xs.w);
-                const float bnd = cand_bound<NC>(p0, p1, p2, lt, cw, bb);
-                sm.LB[t] = bnd;
-                if (bnd < lmin) { lmin = bnd; tseed = t; }
+            if (unit16) {
+                const float4 *ub = (NC == 4 ? g_ub4 : g_ub3) + lane;
+#pragma unroll (NITER > 1 ? 1 : 2)
+                for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM, ub += TEAM) {
+                    const float4 q = __ldg(ub);
+                    const uint32_t o = __float_as_uint(q.w);
+                    const float4 p0 = sm.S[o & 0xFFu];
+                    const float4 p1 = sm.S[(o >> 8) & 0xFFu];
+                    const float4 p2 = (NC == 4) ? sm.S[o >> 16] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    const float bnd = unit_bound<NC>(p0, p1, p2, q, xs, cw, bb);
+                    sm.LB[t] = bnd;
+                    if (bnd < lmin) { lmin = bnd; tseed = t; }
+                }
+            } else {
+                for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
+                    const uint32_t e = __ldg(tbl + t);
+                    const float4 p0 = sm.S[e & 0xFu];
+                    const float4 p1 = sm.S[(e >> 4) & 0xFFu];
+                    const float4 p2 = (NC == 4) ? sm.S[(e >> 12) & 0xFFu] : make_float4(0.f, 0.f, 0.f, 0.f);
+                    const float bnd = cand_bound<NC>(p0, p1, p2, lb_terms<NC>(p0.w, p1.w, p2.w, xs.w), cw, bb);
+                    sm.LB[t] = bnd;
+                    if (bnd < lmin) { lmin = bnd; tseed = t; }
+                }
             }
             // 2. seeds: every lane's smallest bound, evaluated exactly; the
             // threshold is the smallest error reached (never above run)
@@ -1113,18 +1154,21 @@ __device__ __forceinline__ void cluster_block(const Team<TEAM> &tm, TeamSmem &sm
     tm.sync();
 }
 
-// (A, -2B, alpha, 1/det) of exact weight-lane terms w = (alpha, beta, gamma,
-// factor), A = alpha + beta + 2 gamma, B = alpha + gamma: det of the f32 values
-// is exact in double (products of two 24-bit significands), A, B and 1/det are
-// rounded once to f32.
-__device__ __forceinline__ float4 bound_terms(const float4 w) {
+// (F1, r, C, offsets) of unit_bound from exact weight-lane terms w = (alpha,
+// beta, gamma, factor) of a weight-1, 16-point set (W = 16): A = alpha + beta +
+// 2 gamma, B = alpha + gamma, f = 1/det.  det of the f32 values is exact in
+// double (products of two 24-bit significands); each term is rounded once.
+__device__ __forceinline__ float4 unit_terms(const float4 w, uint32_t offs) {
     const double al = w.x, be = w.y, ga = w.z;
     const double det = al * be - ga * ga;
-    const float f = det > 0.0 ? (float)(1.0 / det) : __int_as_float(0x7fc00000);  // NaN: no bound
-    return make_float4((float)(al + be + 2.0 * ga), (float)(-2.0 * (al + ga)), w.x, f);
+    const double A = al + be + 2.0 * ga;
+    const float nan = __int_as_float(0x7fc00000);  // no bound
+    if (!(det > 0.0)) return make_float4(nan, 0.0f, nan, __uint_as_float(offs));
+    return make_float4((float)(-A / det), (float)(2.0 * (al + ga) / A), (float)(-(al + 0x1p-13) / det),
+                       __uint_as_float(offs));
 }
 
-// Fill the bound terms g_lb4 / g_lb3 from this TU's loop-order candidate
+// Fill the bound terms g_ub4 / g_ub3 from this TU's loop-order candidate
 // lists: the w-lane sums of a 16-point, weight-1 set are S(a,b).w = b - a
 // (exact small integers), and wterms4 / wterms3 are the reference's f32 code.
 static __global__ void k_unit_terms() {
@@ -1132,12 +1176,14 @@ static __global__ void k_unit_terms() {
     if (t < kCand4) {
         int i, j, k;
         decode_entry(g_cand16[t], i, j, k);
-        g_lb4[t] = bound_terms(wterms4((float)i, (float)(j - i), (float)(k - j), 16.0f));
+        const uint32_t offs = (uint32_t)tri_idx(0, i) | (uint32_t)tri_idx(i, j) << 8 | (uint32_t)tri_idx(j, k) << 16;
+        g_ub4[t] = unit_terms(wterms4((float)i, (float)(j - i), (float)(k - j), 16.0f), offs);
     }
     if (t < kCand3) {
         int i, j, k;
         decode_entry(g_cand16[kCand4 + 1 + t], i, j, k);
-        g_lb3[t] = bound_terms(wterms3((float)i, (float)(j - i), 16.0f));
+        const uint32_t offs = (uint32_t)tri_idx(0, i) | (uint32_t)tri_idx(i, j) << 8;
+        g_ub3[t] = unit_terms(wterms3((float)i, (float)(j - i), 16.0f), offs);
     }
 }
 
