@@ -44,9 +44,8 @@ static __device__ uint32_t g_cand16[kCand4 + 1 + kCand3 + 1];
 // Lower-bound terms (F1, r, C, S offsets) of the g_cand16 candidates of a
 // 16-colour set whose weights are all exactly 1 (the w lanes of the partial
 // sums are then the counts i, j-i, k-j), from the reference's f32 alpha2,
-// beta2, alphabeta (see unit_terms and unit_bound; F1 = C = NaN when
-// det <= 0: no bound).  The w lane holds the bits i | S(i,j) << 8 |
-// S(j,k) << 16 (table offsets, one byte each).
+// beta2, alphabeta (see unit_terms and unit_bound).  The w lane holds the
+// bits i | S(i,j) << 8 | S(j,k) << 16 (table offsets, one byte each).
 static __device__ float4 g_ub4[kCand4 + 1];
 static __device__ float4 g_ub3[kCand3 + 1];
 
@@ -781,6 +780,7 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
                     if (bnd < lmin) { lmin = bnd; tseed = t; }
                 }
             } else {
+#pragma unroll (NITER > 1 ? 1 : 2)
                 for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) {
                     const uint32_t e = __ldg(tbl + t);
                     const float4 p0 = sm.S[e & 0xFu];
@@ -1158,12 +1158,23 @@ __device__ __forceinline__ void cluster_block(const Team<TEAM> &tm, TeamSmem &sm
 // beta, gamma, factor) of a weight-1, 16-point set (W = 16): A = alpha + beta +
 // 2 gamma, B = alpha + gamma, f = 1/det.  det of the f32 values is exact in
 // double (products of two 24-bit significands); each term is rounded once.
-__device__ __forceinline__ float4 unit_terms(const float4 w, uint32_t offs) {
+//
+// det = 0 exactly when every point is in one cluster (one interpolation
+// weight l; the f32 constants keep alpha : beta : gamma = l^2 : (1-l)^2 :
+// l(1-l) exactly, as 4/9 and 2/9 are 4 and 2 times 1/9 in f32).  The fit is
+// then a single colour c = l a + (1-l) b, whose error sum_c w_c (W c^2 -
+// 2 X c) is at least -Z/W; the reference's rounded ax, bx move it by at most
+// 4 u sum_c w_c X_c (a, b in [0,1]), inside eps1.  So such a candidate gets
+// the flat bound -(1 + 2^-10) Z/W - eps1 (F1 = 0), which the fitted
+// endpoints of a textured block beat, instead of no bound.
+__device__ __forceinline__ float4 unit_terms(const float4 w, uint32_t offs, bool one_cluster) {
     const double al = w.x, be = w.y, ga = w.z;
     const double det = al * be - ga * ga;
     const double A = al + be + 2.0 * ga;
     const float nan = __int_as_float(0x7fc00000);  // no bound
-    if (!(det > 0.0)) return make_float4(nan, 0.0f, nan, __uint_as_float(offs));
+    if (!(det > 0.0))
+        return one_cluster ? make_float4(0.0f, 0.0f, (float)(-(1.0 + 0x1p-10) / 16.0), __uint_as_float(offs))
+                           : make_float4(nan, 0.0f, nan, __uint_as_float(offs));
     return make_float4((float)(-A / det), (float)(2.0 * (al + ga) / A), (float)(-(al + 0x1p-13) / det),
                        __uint_as_float(offs));
 }
@@ -1177,13 +1188,15 @@ static __global__ void k_unit_terms() {
         int i, j, k;
         decode_entry(g_cand16[t], i, j, k);
         const uint32_t offs = (uint32_t)tri_idx(0, i) | (uint32_t)tri_idx(i, j) << 8 | (uint32_t)tri_idx(j, k) << 16;
-        g_ub4[t] = unit_terms(wterms4((float)i, (float)(j - i), (float)(k - j), 16.0f), offs);
+        const bool one = (i == 16) + (j - i == 16) + (k - j == 16) + (16 - k == 16) == 1;
+        g_ub4[t] = unit_terms(wterms4((float)i, (float)(j - i), (float)(k - j), 16.0f), offs, one);
     }
     if (t < kCand3) {
         int i, j, k;
         decode_entry(g_cand16[kCand4 + 1 + t], i, j, k);
         const uint32_t offs = (uint32_t)tri_idx(0, i) | (uint32_t)tri_idx(i, j) << 8;
-        g_ub3[t] = unit_terms(wterms3((float)i, (float)(j - i), 16.0f), offs);
+        const bool one = (i == 16) + (j - i == 16) + (16 - j == 16) == 1;
+        g_ub3[t] = unit_terms(wterms3((float)i, (float)(j - i), 16.0f), offs, one);
     }
 }
 
