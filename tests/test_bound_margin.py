@@ -58,6 +58,13 @@ def bounds(P0, P1, P2, xs, w, nc):
         acc0 = fma(A, s1, fma(B2, s2, (al * Z).astype(f32)))
         lb0 = (-f * acc0).astype(f32)
         margin = (f * kb + eps1).astype(f32)
+        # one-cluster candidates get the flat bound -(1 + 2^-10) Z / W - eps1
+        cnt = [P0[:, 3], P1[:, 3], P2[:, 3]] if nc == 4 else [P0[:, 3], P1[:, 3]]
+        one = sum((c == xs[3]).astype(int) for c in cnt) == 1
+        rw = (f32(1) / xs[3]).astype(f32)
+        lbm = np.where(one, fma((-(f32(1) + f32(2.0 ** -10)) * Z).astype(f32), rw, -eps1), lbm)
+        lb0 = np.where(one, (-Z * rw).astype(f32), lb0)
+        margin = np.where(one, (f32(2.0 ** -10) * Z * rw + eps1).astype(f32), margin)
     return lbm, lb0, margin
 
 

@@ -37,6 +37,10 @@ constexpr int kCand4 = 967, kCand3 = 151;
 static __device__ uint32_t g_cand[kCand4 + 1 + kCand3 + 1];
 static __constant__ uint32_t c_ncand4[17];
 static __constant__ uint32_t c_ncand3[17];
+// Positions, in the list an n-colour set uses, of its candidates with every
+// point in one cluster: compress4 (0,0,n) and (0,n,n), compress3 (0,n).
+static __constant__ uint16_t c_one4[17][2];
+static __constant__ uint16_t c_one3[17];
 // The same candidates in the reference's loop order (i, j, k nested), used for
 // 16-colour sets: a round of consecutive candidates then mostly shares S(0,i)
 // and S(i,j) and reads S(j,k) at consecutive addresses.
@@ -798,8 +802,26 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
                 sm.LB[tseed] = __int_as_float(0x7f800000);  // already evaluated
             }
             const uint32_t ngroups = (ncand + 3u) >> 2;
-            if (lane == 0)
+            if (lane == 0) {
                 for (uint32_t t = ncand; t < 4u * ngroups; ++t) sm.LB[t] = __int_as_float(0x7f800000);
+                if (!unit16 && NITER == 1) {  // (the iterative kernels spill with it)
+                    // one-cluster candidates: the flat bound of unit_terms with W =
+                    // xs.w (their rounded alpha : beta : gamma are within a few u W of
+                    // l^2 : (1-l)^2 : l(1-l), moving the error by at most 32 u W sum w
+                    // on [0,1]^2, inside eps1; 2^-10 covers the approximate 1/W).  A
+                    // seed among them may be written back to infinity, or evaluated
+                    // again: either is harmless.
+                    float rw;
+                    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(rw) : "f"(xs.w));
+                    const float flat = __fmaf_rn(-(1.0f + 0x1p-10f) * bb.z, rw, -bb.eps1);
+                    if (NC == 4) {
+                        sm.LB[c_one4[count][0]] = flat;
+                        sm.LB[c_one4[count][1]] = flat;
+                    } else {
+                        sm.LB[c_one3[count]] = flat;
+                    }
+                }
+            }
             float thr = ob.err;
 #pragma unroll
             for (int off = TEAM / 2; off > 0; off >>= 1) thr = fminf(thr, tm.shfl_xor(thr, off));
@@ -1255,6 +1277,23 @@ static inline cudaError_t upload_tables_this_tu(const uint32_t lut[4][256][2]) {
     if ((e = cudaMemcpyToSymbol(g_cand16, loop_tbl, sizeof(loop_tbl))) != cudaSuccess) return e;
     if ((e = cudaMemcpyToSymbol(c_ncand4, nc4, sizeof(nc4))) != cudaSuccess) return e;
     if ((e = cudaMemcpyToSymbol(c_ncand3, nc3, sizeof(nc3))) != cudaSuccess) return e;
+    // positions of the one-cluster candidates in the list each count uses
+    uint16_t one4[17][2] = {}, one3[17] = {};
+    auto find = [](const uint32_t *list, int n, uint32_t key, uint32_t mask) {
+        for (int t = 0; t < n; ++t)
+            if ((list[t] & mask) == key) return (uint16_t)t;
+        return (uint16_t)0;
+    };
+    for (int n = 1; n <= 16; ++n) {
+        const uint32_t *l4 = n == 16 ? loop_tbl : tbl;
+        const uint32_t *l3 = n == 16 ? loop_tbl + kCand4 + 1 : tbl + kCand4 + 1;
+        const uint32_t m4 = 0xFFFFFu, m3 = 0xFFFu;  // the i, S(i,j), S(j,k) fields
+        one4[n][0] = find(l4, kCand4, (uint32_t)tri_idx(0, 0) << 4 | (uint32_t)tri_idx(0, n) << 12, m4);
+        one4[n][1] = find(l4, kCand4, (uint32_t)tri_idx(0, n) << 4 | (uint32_t)tri_idx(n, n) << 12, m4);
+        one3[n] = find(l3, kCand3, (uint32_t)tri_idx(0, n) << 4, m3);
+    }
+    if ((e = cudaMemcpyToSymbol(c_one4, one4, sizeof(one4))) != cudaSuccess) return e;
+    if ((e = cudaMemcpyToSymbol(c_one3, one3, sizeof(one3))) != cudaSuccess) return e;
     k_unit_terms<<<(kCand4 + 255) / 256, 256>>>();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
