@@ -18,7 +18,10 @@ no benchmark inputs.
           operations = reference candidate evaluations x ops per candidate;
           the kernel skips, exactly, the candidates whose error lower bound
           exceeds an error already reached, so this is a reference-equivalent
-          rate) plus the HBM roofline of the same launch (80 B per block).
+          rate) plus the HBM roofline of the same launch (80 B per block) and
+          the issue-slot view (warp instructions per launch from the committed
+          ncu capture / the live launch time, against one warp instruction per
+          SM sub-partition per clock).
   cpu_baseline  the CPU oracle (a C restatement of the reference's block
           path) on all host cores, one block row per task as rayon does.
   extra   the other formats / algorithms of the benchmark configurations,
@@ -396,7 +399,7 @@ def run_ours(args):
                      "unit": "TFLOP/s", "frac": round(achieved_tops / fp32_peak_tops, 4), "traffic": None,
                      "work": "%d FP32 ops per launch = the reference's candidate evaluations x %d (compress4); "
                              "the kernel bounds every candidate's error from below and evaluates the exact error "
-                             "only where the bound does not exclude it (about 2 %%), so this is the "
+                             "only where the bound does not exclude it (about 4 %%), so this is the "
                              "reference-equivalent rate, not the FP32 rate executed (issue-slot use: "
                              "profiles/k_cluster_bc3_2048.md)" % (ops, OPS_CAND4),
                      "peak_basis": "nominal: 152 SMs x 128 FP32 lanes x %.0f MHz (sm_max_mhz)" % sm_max_mhz},
@@ -405,6 +408,16 @@ def run_ours(args):
                          "basis": "80 B per block (64 B RGBA8 + 16 B BC3) x %d blocks; peak %s" % (nb, peak_kind)},
         "clocks": clk,
     }
+    inst = dram_traffic().get("bc3_cluster_%d_inst" % size)
+    if inst is not None:
+        issue_peak = 152 * 4 * sm_max_mhz * 1e6 / 1e9
+        issue_achieved = inst / (ms_step * 1e-3) / 1e9
+        line["roofline_issue"] = {
+            "bound": "issue", "achieved": round(issue_achieved, 1), "peak": round(issue_peak, 1), "unit": "Ginst/s",
+            "frac": round(issue_achieved / issue_peak, 4),
+            "basis": "%d warp instructions per launch (smsp__inst_executed.sum, profiles/k_cluster_bc3_2048.md) / "
+                     "this run's launch time; peak 152 SMs x 4 sub-partitions x 1 warp instruction per clock at "
+                     "%.0f MHz" % (inst, sm_max_mhz)}
     traffic = dram_traffic().get("bc3_cluster_%d" % size)
     if traffic is not None:
         line["roofline"]["traffic"] = traffic
