@@ -588,7 +588,7 @@ def batched(torch, tx, args, n_textures=1000):
            "gain_vs_per_call_graph": round(percall_graph_ms / batch_ms, 2),
            "identical_to_per_call": identical, "tuning": chosen.as_dict(),
            "setup_s": {"generate_and_mips": round(gen_s, 2), "autotune": round(tune_s, 2)},
-           "launch": "one CUDA graph replay: counter memset + persistent lane kernel + persistent team kernel"}
+           "launch": "one CUDA graph replay: counter memset + persistent lane kernel + one persistent team kernel per (format, iterative) class"}
     b.close()
     del ts, gb, gp
     torch.cuda.empty_cache()
