@@ -225,7 +225,7 @@ int fail_batch(cudaError_t e) {
 
 // (Re)build the unit queues for the current tuning and upload them.
 int build_units(tx_batch *b) {
-    std::vector<uint2> lane, cls[tx::kTeamClasses], team_iter;
+    std::vector<uint2> lane, cls[tx::kTeamClasses], team;
     const uint32_t lane_span = 32u * (uint32_t)b->tuning.lane_blocks_per_lane;
     const uint32_t team_span = (uint32_t)b->tuning.team_blocks_per_unit;
     for (uint32_t i = 0; i < b->desc.size(); ++i) {
@@ -239,13 +239,13 @@ int build_units(tx_batch *b) {
     }
     for (int c = 0; c < tx::kTeamClasses; ++c) {  // class order: iterative (most expensive) first
         b->team_counts[c] = (uint32_t)cls[c].size();
-        team_iter.insert(team_iter.end(), cls[c].begin(), cls[c].end());
+        team.insert(team.end(), cls[c].begin(), cls[c].end());
     }
     cudaFree(b->d_lane_units);
     cudaFree(b->d_team_units);
     b->d_lane_units = b->d_team_units = nullptr;
     b->n_lane = (uint32_t)lane.size();
-    b->n_team = (uint32_t)team_iter.size();
+    b->n_team = (uint32_t)team.size();
     cudaError_t e;
     if (b->n_lane) {
         if ((e = cudaMalloc(&b->d_lane_units, lane.size() * sizeof(uint2))) != cudaSuccess) return fail_batch(e);
@@ -253,8 +253,8 @@ int build_units(tx_batch *b) {
             return fail_batch(e);
     }
     if (b->n_team) {
-        if ((e = cudaMalloc(&b->d_team_units, team_iter.size() * sizeof(uint2))) != cudaSuccess) return fail_batch(e);
-        if ((e = cudaMemcpy(b->d_team_units, team_iter.data(), team_iter.size() * sizeof(uint2), cudaMemcpyHostToDevice)) !=
+        if ((e = cudaMalloc(&b->d_team_units, team.size() * sizeof(uint2))) != cudaSuccess) return fail_batch(e);
+        if ((e = cudaMemcpy(b->d_team_units, team.data(), team.size() * sizeof(uint2), cudaMemcpyHostToDevice)) !=
             cudaSuccess)
             return fail_batch(e);
     }
