@@ -488,7 +488,12 @@ def extra_cases(tx, names=None):
     return out
 
 
-def time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak):
+# warp instructions per launch of a case's kernel, from profiles/dram_traffic.txt
+CASE_INST = {"c1_bc3_range": "bc3_range_2048_inst", "c2_bc4_r8": "bc4_r8_4096_inst",
+             "bc1_iter_cluster": "bc1_iter_2048_inst", "c1_bc3_cluster": "bc3_cluster_2048_inst"}
+
+
+def time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak, inst=None):
     from texpresso_gb300 import workloads
     r = DeviceRun(torch, tx, fmt, [img], p, channels=ch)
     ms, launches = r.time(steps, 3)
@@ -504,6 +509,12 @@ def time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak):
         ops = cluster_ops(rgba_img, fmt)
         tops = ops / (ms_step * 1e-3) / 1e12
         rec["fp32"] = {"achieved_tops": round(tops, 3), "frac": round(tops / fp32_peak, 4)}
+    if inst:
+        # these kernels are bound by instruction issue, not HBM: the executed view
+        issue_peak = fp32_peak * 1e3 / 32.0  # Ginst/s: one warp instruction per scheduler and clock
+        gi = inst / (ms_step * 1e-3) / 1e9
+        rec["issue"] = {"achieved_ginst_s": round(gi, 1), "frac": round(gi / issue_peak, 4),
+                        "inst_per_launch": inst}
     del r
     torch.cuda.empty_cache()
     return rec
@@ -515,7 +526,8 @@ def extras(torch, tx, oracle, args, hbm_peak, fp32_peak):
     out = {}
     steps = max(20, min(200, args.steps))
     for key, label, fmt, img, p, alg, ch in extra_cases(tx):
-        rec = time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak)
+        rec = time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak,
+                        dram_traffic().get(CASE_INST.get(key, ""), None))
         rgba_img = img if ch == 4 else workloads.expand_to_rgba(img)
         op = oracle.make_params(alg, tuple(p.weights), p.weigh_colour_by_alpha)
         cv, _, _ = cpu_rate(oracle, fmt, rgba_img, op, 2.5)
@@ -716,7 +728,8 @@ def run_case(args):
     hbm_peak, sm_max_mhz, _ = peaks()
     fp32_peak = 152 * 128 * sm_max_mhz * 1e6 / 1e12
     (key, label, fmt, img, p, alg, ch), = extra_cases(tx, [args.case])
-    rec = time_case(torch, tx, fmt, img, p, alg, ch, args.steps, hbm_peak, fp32_peak)
+    rec = time_case(torch, tx, fmt, img, p, alg, ch, args.steps, hbm_peak, fp32_peak,
+                    dram_traffic().get(CASE_INST.get(key, ""), None))
     rec["case"] = key
     rec["label"] = label
     print(json.dumps(rec), flush=True)
