@@ -250,39 +250,61 @@ struct AlphaBook {
     uint32_t val_lo, val_hi;   // code value at sorted positions 0-3 / 4-7
 };
 
-__device__ __forceinline__ void cmpx(uint32_t &a, uint32_t &b) {
-    const uint32_t lo = min(a, b), hi = max(a, b);
-    a = lo;
-    b = hi;
+// 0xFF in every byte where x == y, else 0x00.
+__device__ __forceinline__ uint32_t bytes_eq(uint32_t x, uint32_t y) {
+    const uint32_t H = 0x80808080u, d = x ^ y;
+    return prmt(~(((d | H) - 0x01010101u) | d) & H, 0u, 0xBA98u);
 }
 
-// Book of any 8 codes (the 7-value book: codes 0 and 1 are min5 and max5,
-// alpha.rs:237-239, anywhere among the interpolants of min7..max7).
-__device__ __forceinline__ AlphaBook make_book(const uint32_t (&codes)[8]) {
-    uint32_t k[8];  // value << 3 | index
-#pragma unroll
-    for (int j = 0; j < 8; ++j) k[j] = (codes[j] << 3) | (uint32_t)j;
-    // Batcher's odd-even merge sort of 8
-    cmpx(k[0], k[1]); cmpx(k[2], k[3]); cmpx(k[4], k[5]); cmpx(k[6], k[7]);
-    cmpx(k[0], k[2]); cmpx(k[1], k[3]); cmpx(k[4], k[6]); cmpx(k[5], k[7]);
-    cmpx(k[1], k[2]); cmpx(k[5], k[6]);
-    cmpx(k[0], k[4]); cmpx(k[3], k[7]); cmpx(k[1], k[5]); cmpx(k[2], k[6]);
-    cmpx(k[1], k[4]); cmpx(k[3], k[6]);
-    cmpx(k[2], k[4]); cmpx(k[3], k[5]);
-    cmpx(k[3], k[4]);
-#pragma unroll
-    for (int j = 1; j < 8; ++j) k[j] = ((k[j] ^ k[j - 1]) < 8u) ? k[j - 1] : k[j];  // equal value: merge
+// The 7-value book (alpha.rs:237-242) without a sort: codes 2-7, the
+// interpolants of min7..max7, rise strictly (max7 - min7 >= 7), and min5 <
+// max5 (indices 0 and 1) go in front of the interpolants of equal value, so
+// in (value, index) order min5 sits after the p0 interpolants below it and
+// max5 after the p1 - 1 below it and min5.  One nibble selector per sorted
+// position then gathers values and indices with prmt from the bytes
+// [c2 c3 c4 c5 | c6 c7 min5 max5].  An interpolant equal to min5 or max5
+// directly follows it and takes its index (the merge of make_book; values
+// are distinct otherwise, so merges never chain).  Thresholds between
+// neighbours (a, b) are (a + b + 2 - [ib < ia]) / 2 capped at 255: the
+// rounded-up byte average, plus one when a + b is even and ib > ia.
+__device__ __forceinline__ AlphaBook make_book7(uint32_t min5, uint32_t max5, const uint32_t (&c)[8]) {
+    const uint32_t A = c[2] | c[3] << 8 | c[4] << 16 | c[5] << 24;
+    const uint32_t B6 = c[6] | c[7] << 8 | 0xFFFF0000u;  // padding bytes never count as below
+    const uint32_t n5 = min5 * 0x01010101u, x5 = max5 * 0x01010101u;
+    const uint32_t p0 = (uint32_t)(__popc(~bytes_ge(A, n5)) + __popc(~bytes_ge(B6, n5))) >> 3;
+    const uint32_t p1 = ((uint32_t)(__popc(~bytes_ge(A, x5)) + __popc(~bytes_ge(B6, x5))) >> 3) + 1u;
+    uint32_t sel = 0x76543210u - (0x11111111u << (4 * p0 + 4)) - (p1 < 7u ? 0x11111111u << (4 * p1 + 4) : 0u);
+    sel = (sel & ~(0xFu << (4 * p0))) | (6u << (4 * p0));
+    sel = (sel & ~(0xFu << (4 * p1))) | (7u << (4 * p1));
+    const uint32_t B = (B6 & 0xFFFFu) | min5 << 16 | max5 << 24;
     AlphaBook bk;
+    bk.val_lo = prmt(A, B, sel & 0xFFFFu);
+    bk.val_hi = prmt(A, B, sel >> 16);
+    const uint32_t ilo = prmt(0x05040302u, 0x01000706u, sel & 0xFFFFu);
+    const uint32_t ihi = prmt(0x05040302u, 0x01000706u, sel >> 16);
+    // merge: equal to the predecessor's value -> the predecessor's index
+    const uint32_t eq_lo = bytes_eq(bk.val_lo, prmt(bk.val_lo, ~bk.val_lo, 0x2104u));
+    const uint32_t eq_hi = bytes_eq(bk.val_hi, prmt(bk.val_lo, bk.val_hi, 0x6543u));
+    bk.idx_lo = (ilo & ~eq_lo) | (prmt(ilo, 0u, 0x2104u) & eq_lo);
+    bk.idx_hi = (ihi & ~eq_hi) | (prmt(ilo, ihi, 0x6543u) & eq_hi);
+    // thresholds of the pairs (s, s+1), s = 0-3 in the low word, 4-6 in the high
+    const uint32_t rv_lo = prmt(bk.val_lo, bk.val_hi, 0x4321u), rv_hi = bk.val_hi >> 8;
+    const uint32_t rx_lo = prmt(bk.idx_lo, bk.idx_hi, 0x4321u), rx_hi = bk.idx_hi >> 8;
+    uint32_t T[2];
 #pragma unroll
-    for (int j = 0; j < 7; ++j) {
-        const uint32_t a = k[j] >> 3, b = k[j + 1] >> 3;
-        const uint32_t T = min((a + b + 2u - ((k[j + 1] & 7u) < (k[j] & 7u) ? 1u : 0u)) >> 1, 255u);
-        bk.t[j] = T * 0x01010101u;
+    for (int w = 0; w < 2; ++w) {
+        const uint32_t a = w ? bk.val_hi : bk.val_lo, b = w ? rv_hi : rv_lo;
+        const uint32_t xa = w ? bk.idx_hi : bk.idx_lo, xb = w ? rx_hi : rx_lo;
+        const uint32_t up = (a | b) - (((a ^ b) >> 1) & 0x7F7F7F7Fu);   // (a + b + 1) >> 1
+        const uint32_t ge = ~(((xb | 0x08080808u) - xa) >> 3) ^ 0xFFFFFFFFu;  // bit 0: ib >= ia
+        // + 1 where a + b is even and ib > ia (ib == ia only for merged equal
+        // values, where a + b is even too and the rule adds one as well)
+        uint32_t inc = ~(a ^ b) & ge & 0x01010101u;
+        inc &= ~bytes_eq(up, 0xFFFFFFFFu);  // 255 + 1 is capped at 255
+        T[w] = up + inc;
     }
-    bk.idx_lo = (k[0] & 7u) | ((k[1] & 7u) << 8) | ((k[2] & 7u) << 16) | ((k[3] & 7u) << 24);
-    bk.idx_hi = (k[4] & 7u) | ((k[5] & 7u) << 8) | ((k[6] & 7u) << 16) | ((k[7] & 7u) << 24);
-    bk.val_lo = (k[0] >> 3) | ((k[1] >> 3) << 8) | ((k[2] >> 3) << 16) | ((k[3] >> 3) << 24);
-    bk.val_hi = (k[4] >> 3) | ((k[5] >> 3) << 8) | ((k[6] >> 3) << 16) | ((k[7] >> 3) << 24);
+#pragma unroll
+    for (int s = 0; s < 7; ++s) bk.t[s] = prmt(T[s >> 2], 0u, (uint32_t)(s & 3) * 0x1111u);
     return bk;
 }
 
@@ -388,7 +410,7 @@ __device__ __forceinline__ uint2 encode_bc3_alpha(const uint32_t (&v)[4], uint32
     uint32_t i5[4], i7[4];
     // errors compared without their common x^2 part
     const int e5 = fit_book(v, vm, make_book5((uint32_t)min5, (uint32_t)max5, c5), i5);
-    const int e7 = fit_book(v, vm, make_book(c7), i7);
+    const int e7 = fit_book(v, vm, make_book7((uint32_t)min5, (uint32_t)max5, c7), i7);
     uint32_t out[4];
     if (e5 <= e7) {
         // write_alpha_block5: a0 > a1 cannot occur after fix_range; kept for fidelity
