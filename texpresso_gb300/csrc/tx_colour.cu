@@ -89,7 +89,22 @@ static cudaError_t launch_range_t(const SrcDesc &src, const DevParams &prm, uint
 template <int FMT, int TEAM, int NITER>
 static cudaError_t launch_cluster_t(const SrcDesc &src, const DevParams &prm, uint8_t *out, size_t nblocks,
                                     cudaStream_t st, const LaunchCfg &cfg) {
-    const int threads = cfg.cluster_threads;
+    // A launch smaller than one wave of 8-team CTAs (SMs x 4 x 8 blocks) runs
+    // in 4-team CTAs: twice as many CTAs spread more evenly over the SMs (for
+    // 4,096 blocks, at most 7 CTAs on an SM against 6.7 on average, instead
+    // of 4 against 3.4), and the slowest SM sets the launch's time.
+    static int sm_count[64] = {};
+    int dev0 = 0;
+    cudaGetDevice(&dev0);
+    if (dev0 < 64 && sm_count[dev0] == 0) {
+        int sms = 0;
+        if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev0) == cudaSuccess && sms > 0)
+            sm_count[dev0] = sms;
+    }
+    int threads = cfg.cluster_threads;
+    if (NITER == 1 && threads == 256 && dev0 < 64 && sm_count[dev0] > 0 &&
+        nblocks < (size_t)sm_count[dev0] * 4 * (256 / TEAM))
+        threads = 128;
     const size_t smem = cluster_smem_bytes(TEAM, threads);
     static bool attr_set[64] = {};
     int dev = 0;
