@@ -45,7 +45,8 @@ def _uniform_table(symbols, length):
 
 
 DC_SYMS = list(range(12))
-AC_SYMS = [0x00, 0xF0] + [(r << 4) | s for r in range(16) for s in range(1, 11)]
+# run/size symbols, ZRL, and the end-of-band runs EOB0..EOB14 of progressive scans
+AC_SYMS = [0x00, 0xF0] + [(r << 4) | s for r in range(16) for s in range(1, 11)] + [r << 4 for r in range(1, 15)]
 DC_TAB = _uniform_table(DC_SYMS, 4)
 AC_TAB = _uniform_table(AC_SYMS, 8)
 
@@ -98,9 +99,10 @@ def _pad(p, h, w):
     return np.pad(p, ((0, h - p.shape[0]), (0, w - p.shape[1])), mode="edge")
 
 
-def encode(img, hv=(1, 1), restart=0, separate_scans=False, q=None):
+def encode(img, hv=(1, 1), restart=0, separate_scans=False, q=None, progressive=None):
     """Baseline JPEG of img (h, w) grey or (h, w, 3) RGB; hv = luma sampling
-    factors (chroma 1x1)."""
+    factors (chroma 1x1).  progressive: a list of (Ss, Se, Ah, Al) scans, DC
+    scans interleaved over all components, AC scans one per component."""
     img = np.asarray(img)
     h, w = img.shape[:2]
     q = np.full(64, 2, np.int64) if q is None else q
@@ -132,7 +134,7 @@ def encode(img, hv=(1, 1), restart=0, separate_scans=False, q=None):
     sof = struct.pack(">BHHB", 8, h, w, nf)
     for k, (fh, fv) in enumerate(factors):
         sof += bytes([k + 1, (fh << 4) | fv, 0])
-    out += b"\xff\xc0" + struct.pack(">H", 2 + len(sof)) + sof
+    out += (b"\xff\xc2" if progressive else b"\xff\xc0") + struct.pack(">H", 2 + len(sof)) + sof
     for tc, tab in ((0, DC_TAB), (1, AC_TAB)):
         body = bytes([tc << 4]) + bytes(tab[0]) + bytes(tab[1])
         out += b"\xff\xc4" + struct.pack(">H", 2 + len(body)) + body
@@ -166,7 +168,120 @@ def encode(img, hv=(1, 1), restart=0, separate_scans=False, q=None):
         bw.flush()
         return seg + bytes(bw.out)
 
-    if separate_scans:
+    def pscan(comp_ids, ss, se, ah, al):
+        sos = bytes([len(comp_ids)])
+        for k in comp_ids:
+            sos += bytes([k + 1, 0x00])
+        sos += bytes([ss, se, (ah << 4) | al])
+        seg = b"\xff\xda" + struct.pack(">H", 2 + len(sos)) + sos
+        bw = _BitWriter()
+        if len(comp_ids) == 1:
+            k = comp_ids[0]
+            units = [[(k, by, bx)] for by in range(extents[k][0]) for bx in range(extents[k][1])]
+        else:
+            units = [[(k, my * factors[k][1] + v, mx * factors[k][0] + u)
+                      for k in comp_ids for v in range(factors[k][1]) for u in range(factors[k][0])]
+                     for my in range(mcuy) for mx in range(mcux)]
+        st = {"eobrun": 0, "be": [], "pred": {k: 0 for k in comp_ids}}
+
+        def sym(v):
+            code, ln = AC_TAB[2][v]
+            bw.put(code, ln)
+
+        def emit_eobrun():
+            if st["eobrun"]:
+                n = st["eobrun"].bit_length() - 1
+                sym(n << 4)
+                if n:
+                    bw.put(st["eobrun"] & ((1 << n) - 1), n)
+                st["eobrun"] = 0
+                for b in st["be"]:
+                    bw.put(b, 1)
+                st["be"] = []
+
+        marker = 0
+        for n, unit in enumerate(units):
+            if restart and n and n % restart == 0:
+                emit_eobrun()
+                bw.flush()
+                bw.out += bytes([0xFF, 0xD0 + marker])
+                marker = (marker + 1) & 7
+                st["pred"] = {k: 0 for k in comp_ids}
+            for k, by, bx in unit:
+                zz = comp_blocks[k][by, bx]
+                if ss == 0:
+                    if ah == 0:
+                        v = int(zz[0]) >> al
+                        d = v - st["pred"][k]
+                        st["pred"][k] = v
+                        c = _category(d)
+                        code, ln = DC_TAB[2][c]
+                        bw.put(code, ln)
+                        if c:
+                            bw.put(d if d > 0 else d + (1 << c) - 1, c)
+                    else:
+                        bw.put((int(zz[0]) >> al) & 1, 1)
+                elif ah == 0:  # AC first (T.81 G.1.2.2, as libjpeg's encoder)
+                    r = 0
+                    for z in range(ss, se + 1):
+                        a = abs(int(zz[z])) >> al
+                        if a == 0:
+                            r += 1
+                            continue
+                        emit_eobrun()
+                        while r > 15:
+                            sym(0xF0)
+                            r -= 16
+                        c = a.bit_length()
+                        sym((r << 4) | c)
+                        bw.put(a if zz[z] > 0 else (~a) & ((1 << c) - 1), c)
+                        r = 0
+                    if r:
+                        st["eobrun"] += 1
+                        if st["eobrun"] == 0x7FFF:
+                            emit_eobrun()
+                else:  # AC refinement (T.81 G.1.2.3, as libjpeg's encoder)
+                    absv = [abs(int(zz[z])) >> al for z in range(64)]
+                    eob = max([z for z in range(ss, se + 1) if absv[z] == 1], default=-1)
+                    r, br = 0, []
+                    for z in range(ss, se + 1):
+                        t = absv[z]
+                        if t == 0:
+                            r += 1
+                            continue
+                        while r > 15 and z <= eob:
+                            emit_eobrun()
+                            sym(0xF0)
+                            r -= 16
+                            for b in br:
+                                bw.put(b, 1)
+                            br = []
+                        if t > 1:
+                            br.append(t & 1)
+                            continue
+                        emit_eobrun()
+                        sym((r << 4) | 1)
+                        bw.put(0 if zz[z] < 0 else 1, 1)
+                        for b in br:
+                            bw.put(b, 1)
+                        br, r = [], 0
+                    if r or br:
+                        st["eobrun"] += 1
+                        st["be"] += br
+                        if st["eobrun"] == 0x7FFF:
+                            emit_eobrun()
+        emit_eobrun()
+        bw.flush()
+        return seg + bytes(bw.out)
+
+    if progressive:
+        for ss, se, ah, al in progressive:
+            if ss == 0:
+                out += pscan(list(range(nf)), ss, se, ah, al)
+            else:
+                for k in range(nf):
+                    out += pscan([k], ss, se, ah, al)
+    elif separate_scans:
         for k in range(nf):
             out += scan([k])
     else:
@@ -235,11 +350,40 @@ def test_exact_coefficients_decode_exactly():
         assert np.all(rgba[..., 0] == level)
 
 
+PROGRESSIVE = [
+    [(0, 0, 0, 0), (1, 63, 0, 0)],                                   # spectral selection only
+    [(0, 0, 0, 1), (1, 5, 0, 2), (6, 63, 0, 2), (0, 0, 1, 0),         # libjpeg-like script
+     (1, 63, 2, 1), (1, 63, 1, 0)],
+    [(0, 0, 0, 2), (0, 0, 2, 1), (0, 0, 1, 0), (1, 2, 0, 0), (3, 63, 0, 3),
+     (3, 63, 3, 2), (3, 63, 2, 1), (3, 63, 1, 0)],
+]
+
+
+@pytest.mark.parametrize("script", range(len(PROGRESSIVE)))
+@pytest.mark.parametrize("hv,restart", [((1, 1), 0), ((2, 2), 0), ((2, 1), 2)])
+def test_progressive_decodes_like_baseline(script, hv, restart):
+    """The same quantised coefficients written as a progressive sequence of
+    scans decode to exactly the pixels of the baseline file."""
+    img = _image(29, 45, seed=7 + script)
+    q = np.arange(1, 65, dtype=np.int64) // 8 + 1  # small steps: many coefficients, deep refinement
+    base = jpegio.read_jpeg(encode(img, hv=hv, q=q))[2]
+    prog = jpegio.read_jpeg(encode(img, hv=hv, q=q, restart=restart, progressive=PROGRESSIVE[script]))[2]
+    assert np.array_equal(base, prog)
+
+
+def test_progressive_grey():
+    img = _image(17, 26, seed=9)[..., 0]
+    q = np.full(64, 1, np.int64)
+    base = jpegio.read_jpeg(encode(img, q=q))[2]
+    prog = jpegio.read_jpeg(encode(img, q=q, restart=1, progressive=PROGRESSIVE[1]))[2]
+    assert np.array_equal(base, prog)
+
+
 def test_rejects_what_the_cli_rejects():
     img = _image(8, 8, seed=1)
     data = bytearray(encode(img))
     i = data.index(b"\xff\xc0")
-    data[i + 1] = 0xC2  # progressive
+    data[i + 1] = 0xC9  # arithmetic coding
     with pytest.raises(jpegio.JpegError):
         jpegio.read_jpeg(bytes(data))
     with pytest.raises(jpegio.JpegError):
@@ -270,3 +414,14 @@ def test_read_image_picks_the_decoder_by_extension(tmp_path):
     for bad in ("c.bmp", "noext"):
         with pytest.raises(ValueError):
             image.read_image(tmp_path / bad)
+
+
+def test_progressive_long_end_of_band_runs():
+    """A nearly flat image under coarse steps: most blocks end their bands at
+    once, so the AC scans are mostly end-of-band runs across blocks."""
+    img = np.full((64, 64, 3), 100, np.uint8)
+    img[::7] = 140
+    q = np.full(64, 40, np.int64)
+    base = jpegio.read_jpeg(encode(img, q=q))[2]
+    for script in PROGRESSIVE:
+        assert np.array_equal(jpegio.read_jpeg(encode(img, q=q, progressive=script))[2], base)

@@ -5,10 +5,11 @@ CLI widens the decoder's pixel format to RGBA8 (L8 g -> g,g,g,255; RGB24
 r,g,b -> r,g,b,255) and rejects every other format (CMYK).
 
 This is an independent decoder written against ITU-T T.81 (JPEG) and JFIF
-with numpy; it is not on the GPU path.  It decodes baseline and extended
-sequential Huffman JPEG with 8-bit samples: one or three components, any
-sampling factors, interleaved or single-component scans, restart intervals.
-Progressive, lossless, hierarchical and arithmetic-coded files raise
+with numpy; it is not on the GPU path.  It decodes baseline, extended
+sequential and progressive Huffman JPEG with 8-bit samples (T.81 Annex G:
+spectral selection, successive approximation, end-of-band runs): one or three
+components, any sampling factors, interleaved or single-component scans,
+restart intervals.  Lossless, hierarchical and arithmetic-coded files raise
 JpegError.  The reference's decoder crate (jpeg-decoder 0.3) is not vendored,
 so its exact IDCT and upsampling rounding are not reproduced bit for bit:
 here the inverse DCT is the exact separable cosine transform in float64,
@@ -159,7 +160,7 @@ def _parse(data):
                 n = sum(counts)
                 (dc if tc == 0 else ac)[th] = _Huffman(counts, list(seg[i + 17:i + 17 + n]))
                 i += 17 + n
-        elif m in (0xC0, 0xC1):  # SOF0 baseline, SOF1 extended sequential (Huffman)
+        elif m in (0xC0, 0xC1, 0xC2):  # SOF0 baseline, SOF1 extended sequential, SOF2 progressive
             p, h, w, nf = struct.unpack(">BHHB", seg[:6])
             if p != 8:
                 raise JpegError("%d-bit samples are not supported" % p)
@@ -167,10 +168,9 @@ def _parse(data):
             for k in range(nf):
                 cid, hv, tq = seg[6 + 3 * k], seg[7 + 3 * k], seg[8 + 3 * k]
                 comps.append({"id": cid, "h": hv >> 4, "v": hv & 15, "tq": tq})
-            frame = {"w": w, "h": h, "comps": comps}
-        elif 0xC2 <= m <= 0xCF and m not in (0xC4, 0xC8, 0xCC):
-            raise JpegError("SOF%d (progressive, lossless, hierarchical or arithmetic) is not supported"
-                            % (m - 0xC0))
+            frame = {"w": w, "h": h, "comps": comps, "progressive": m == 0xC2}
+        elif 0xC3 <= m <= 0xCF and m not in (0xC4, 0xC8, 0xCC):
+            raise JpegError("SOF%d (lossless, hierarchical or arithmetic) is not supported" % (m - 0xC0))
         elif m == 0xDD:  # DRI
             (restart,) = struct.unpack(">H", seg[:2])
         elif m == 0xEE and seg[:5] == b"Adobe" and len(seg) >= 12:
@@ -180,9 +180,12 @@ def _parse(data):
                 raise JpegError("scan before frame header")
             ns = seg[0]
             sc = [(seg[1 + 2 * k], seg[2 + 2 * k] >> 4, seg[2 + 2 * k] & 15) for k in range(ns)]
-            if seg[1 + 2 * ns] != 0 or seg[2 + 2 * ns] != 63 or seg[3 + 2 * ns] != 0:
+            ss, se, ah, al = seg[1 + 2 * ns], seg[2 + 2 * ns], seg[3 + 2 * ns] >> 4, seg[3 + 2 * ns] & 15
+            if not frame["progressive"] and (ss, se, ah, al) != (0, 63, 0, 0):
                 raise JpegError("spectral selection / successive approximation in a sequential scan")
-            scans.append((sc, pos, restart, dict(dc), dict(ac)))
+            if frame["progressive"] and (se < ss or se > 63 or (ss == 0) != (se == 0) or (ss > 0 and ns != 1)):
+                raise JpegError("invalid progressive scan parameters")
+            scans.append((sc, pos, restart, dict(dc), dict(ac), (ss, se, ah, al)))
             # skip the entropy-coded segment: to the next marker that is not RSTn or stuffing
             while pos + 1 < len(data):
                 if data[pos] == 0xFF and data[pos + 1] != 0x00 and not 0xD0 <= data[pos + 1] <= 0xD7:
@@ -207,14 +210,16 @@ def _decode_coefficients(data, frame, scans):
         c["cw"] = -(-(-(-frame["w"] * c["h"] // hmax)) // 8)
         c["ch"] = -(-(-(-frame["h"] * c["v"] // vmax)) // 8)
     byid = {c["id"]: c for c in comps}
-    for sc, pos, restart, dct, act in scans:
+    for sc, pos, restart, dct, act, (ss, se, ah, al) in scans:
         sel = []
         for cid, td, ta in sc:
             if cid not in byid:
                 raise JpegError("scan names an unknown component")
-            if td not in dct or ta not in act:
+            # a progressive DC scan uses no AC table, an AC scan no DC table
+            need_dc, need_ac = ss == 0 and ah == 0, se > 0
+            if (need_dc and td not in dct) or (need_ac and ta not in act):
                 raise JpegError("scan uses an undefined Huffman table")
-            sel.append((byid[cid], dct[td], act[ta]))
+            sel.append((byid[cid], dct.get(td), act.get(ta)))
         bits = _Bits(data, pos)
         pred = [0] * len(sel)
         if len(sel) == 1:
@@ -230,13 +235,28 @@ def _decode_coefficients(data, frame, scans):
                             for h in range(c["h"]):
                                 u.append((k, my * c["v"] + v, mx * c["h"] + h))
                     units.append(u)
+        eobrun = [0]
         for n, unit in enumerate(units):
             if restart and n and n % restart == 0:
                 bits.restart()
                 pred = [0] * len(sel)
+                eobrun[0] = 0
             for k, by, bx in unit:
                 c, dt, at = sel[k]
                 blk = c["coef"][by, bx]
+                if frame["progressive"]:
+                    if ss == 0:
+                        if ah == 0:  # DC first scan: the difference, scaled by 2^Al (G.1.2.1)
+                            s = bits.decode(dt)
+                            pred[k] += _extend(bits.bits(s), s)
+                            blk[0] = pred[k] << al
+                        elif bits.bit():  # DC refinement: one more bit
+                            blk[0] |= 1 << al
+                    elif ah == 0:
+                        _ac_first(bits, at, blk, ss, se, al, eobrun)
+                    else:
+                        _ac_refine(bits, at, blk, ss, se, al, eobrun)
+                    continue
                 s = bits.decode(dt)
                 pred[k] += _extend(bits.bits(s), s)
                 blk[0] = pred[k]
@@ -255,6 +275,69 @@ def _decode_coefficients(data, frame, scans):
                     blk[ZIGZAG[z]] = _extend(bits.bits(s), s)
                     z += 1
     return comps, hmax, vmax
+
+
+def _ac_first(bits, table, blk, ss, se, al, eobrun):
+    """First AC scan of one block (T.81 G.1.2.2): run/size symbols scaled by
+    2^Al, ZRL, and end-of-band runs that cover whole blocks."""
+    if eobrun[0] > 0:
+        eobrun[0] -= 1
+        return
+    k = ss
+    while k <= se:
+        rs = bits.decode(table)
+        r, s = rs >> 4, rs & 15
+        if s:
+            k += r
+            if k > se:
+                raise JpegError("coefficient index out of range")
+            blk[ZIGZAG[k]] = _extend(bits.bits(s), s) << al
+            k += 1
+        elif r == 15:
+            k += 16
+        else:
+            eobrun[0] = (1 << r) - 1 + (bits.bits(r) if r else 0)
+            return
+
+
+def _ac_refine(bits, table, blk, ss, se, al, eobrun):
+    """AC refinement scan of one block (T.81 G.1.2.3): a correction bit for
+    every coefficient already non-zero, new coefficients of magnitude 2^Al
+    placed after runs of zero-history coefficients, and end-of-band runs
+    during which only correction bits arrive."""
+    p1, m1 = 1 << al, -1 << al
+    k = ss
+    if eobrun[0] == 0:
+        while k <= se:
+            rs = bits.decode(table)
+            r, s = rs >> 4, rs & 15
+            if s:
+                if s != 1:
+                    raise JpegError("bad refinement symbol")
+                s = p1 if bits.bit() else m1
+            elif r != 15:
+                eobrun[0] = (1 << r) + (bits.bits(r) if r else 0)
+                break
+            while k <= se:
+                z = ZIGZAG[k]
+                if blk[z] != 0:
+                    if bits.bit() and (int(blk[z]) & p1) == 0:
+                        blk[z] += p1 if blk[z] >= 0 else m1
+                else:
+                    r -= 1
+                    if r < 0:
+                        break
+                k += 1
+            if s and k <= se:
+                blk[ZIGZAG[k]] = s
+            k += 1
+    if eobrun[0] > 0:
+        while k <= se:
+            z = ZIGZAG[k]
+            if blk[z] != 0 and bits.bit() and (int(blk[z]) & p1) == 0:
+                blk[z] += p1 if blk[z] >= 0 else m1
+            k += 1
+        eobrun[0] -= 1
 
 
 def _idct_plane(c, q):
