@@ -34,84 +34,107 @@ ZIGZAG = np.array([
     35, 42, 49, 56, 57, 50, 43, 36, 29, 22, 15, 23, 30, 37, 44, 51,
     58, 59, 52, 45, 38, 31, 39, 46, 53, 60, 61, 54, 47, 55, 62, 63], np.int64)
 
+_ZZ = ZIGZAG.tolist()
+
 # C[u, x] = c(u)/2 cos((2x+1) u pi / 16): f = C^T F C is the 8x8 inverse DCT
 _C = np.array([[(math.sqrt(0.5) if u == 0 else 1.0) * 0.5 * math.cos((2 * x + 1) * u * math.pi / 16)
                 for x in range(8)] for u in range(8)])
 
 
 class _Huffman:
-    """Canonical Huffman table (T.81 Annex C) as a (length, code) -> symbol map."""
+    """Canonical Huffman table (T.81 Annex C) with a 16-bit lookup: the next
+    16 bits index (symbol << 8 | code length); length 0 marks no code."""
 
     def __init__(self, counts, symbols):
-        self.lookup = {}
+        fast = [0] * 65536
         code, k = 0, 0
         for length in range(1, 17):
             for _ in range(counts[length - 1]):
-                self.lookup[(length, code)] = symbols[k]
+                lo = code << (16 - length)
+                fast[lo:lo + (1 << (16 - length))] = [(symbols[k] << 8) | length] * (1 << (16 - length))
                 code += 1
                 k += 1
             code <<= 1
+        self.fast = fast
 
 
 class _Bits:
-    """Entropy-coded segment reader: byte stuffing (FF 00) removed, stops at markers."""
+    """Entropy-coded segment reader.  The segment is cut at its RSTn markers
+    into intervals with the byte stuffing (FF 00) removed; bits past an
+    interval's end read as zero (T.81 F.2.2.5)."""
 
     def __init__(self, data, pos):
-        self.data, self.pos = data, pos
-        self.acc, self.n = 0, 0
-        self.marker = None
-
-    def _byte(self):
-        if self.marker is not None or self.pos >= len(self.data):
-            return 0  # past a marker the decoder reads zero bits (T.81 F.2.2.5)
-        b = self.data[self.pos]
-        if b == 0xFF:
-            nxt = self.data[self.pos + 1] if self.pos + 1 < len(self.data) else 0
+        chunks, cur, n = [], [], len(data)
+        while True:
+            f = data.find(b"\xff", pos)
+            if f < 0 or f + 1 >= n:
+                cur.append(data[pos:])
+                break
+            cur.append(data[pos:f])
+            nxt = data[f + 1]
             if nxt == 0x00:
-                self.pos += 2
-                return 0xFF
-            self.marker = nxt
-            return 0
-        self.pos += 1
-        return b
+                cur.append(b"\xff")
+                pos = f + 2
+            elif 0xD0 <= nxt <= 0xD7:
+                chunks.append(b"".join(cur))
+                cur = []
+                pos = f + 2
+            elif nxt == 0xFF:
+                pos = f + 1  # fill byte
+            else:
+                break  # another marker ends the segment
+        chunks.append(b"".join(cur))
+        self.chunks, self.ci = chunks, 0
+        self._start(chunks[0])
+
+    def _start(self, chunk):
+        self.buf, self.pos, self.end = chunk, 0, len(chunk)
+        self.acc, self.n = 0, 0
+
+    def _fill(self, need):
+        while self.n < need:
+            b = self.buf[self.pos:self.pos + 8]
+            if self.pos + 8 > self.end:
+                b = b + bytes(8 - len(b))  # past the end: zero bits
+            self.pos += 8
+            self.acc = (self.acc << 64) | int.from_bytes(b, "big")
+            self.n += 64
 
     def bit(self):
-        if self.n == 0:
-            self.acc, self.n = self._byte(), 8
+        if self.n < 1:
+            self._fill(1)
         self.n -= 1
-        return (self.acc >> self.n) & 1
+        v = (self.acc >> self.n) & 1
+        self.acc &= (1 << self.n) - 1
+        return v
 
-    def bits(self, n):
-        v = 0
-        for _ in range(n):
-            v = (v << 1) | self.bit()
+    def bits(self, k):
+        if k == 0:
+            return 0
+        if self.n < k:
+            self._fill(k)
+        self.n -= k
+        v = self.acc >> self.n
+        self.acc &= (1 << self.n) - 1
         return v
 
     def decode(self, table):
-        code = 0
-        for length in range(1, 17):
-            code = (code << 1) | self.bit()
-            sym = table.lookup.get((length, code))
-            if sym is not None:
-                return sym
-        raise JpegError("bad Huffman code")
+        if self.n < 16:
+            self._fill(16)
+        e = table.fast[(self.acc >> (self.n - 16)) & 0xFFFF]
+        length = e & 0xFF
+        if length == 0:
+            raise JpegError("bad Huffman code")
+        self.n -= length
+        self.acc &= (1 << self.n) - 1
+        return e >> 8
 
     def restart(self):
-        """Skip to and past the next RSTn marker; returns the marker byte."""
-        self.acc, self.n = 0, 0
-        if self.marker is None:
-            while self.pos + 1 < len(self.data) and not (
-                    self.data[self.pos] == 0xFF and 0xD0 <= self.data[self.pos + 1] <= 0xD7):
-                self.pos += 1
-            if self.pos + 1 >= len(self.data):
-                raise JpegError("missing restart marker")
-            self.marker = self.data[self.pos + 1]
-        m = self.marker
-        if not 0xD0 <= m <= 0xD7:
-            raise JpegError("expected a restart marker, found FF%02X" % m)
-        self.pos += 2
-        self.marker = None
-        return m
+        """Move to the interval after the next RSTn marker."""
+        self.ci += 1
+        if self.ci >= len(self.chunks):
+            raise JpegError("missing restart marker")
+        self._start(self.chunks[self.ci])
 
 
 def _extend(v, s):
@@ -187,8 +210,13 @@ def _parse(data):
                 raise JpegError("invalid progressive scan parameters")
             scans.append((sc, pos, restart, dict(dc), dict(ac), (ss, se, ah, al)))
             # skip the entropy-coded segment: to the next marker that is not RSTn or stuffing
-            while pos + 1 < len(data):
-                if data[pos] == 0xFF and data[pos + 1] != 0x00 and not 0xD0 <= data[pos + 1] <= 0xD7:
+            while True:
+                pos = data.find(b"\xff", pos)
+                if pos < 0 or pos + 1 >= len(data):
+                    pos = len(data)
+                    break
+                nxt = data[pos + 1]
+                if nxt != 0x00 and nxt != 0xFF and not 0xD0 <= nxt <= 0xD7:
                     break
                 pos += 1
     if frame is None:
@@ -205,7 +233,7 @@ def _decode_coefficients(data, frame, scans):
     for c in comps:
         # blocks allocated for the interleaved MCU grid (covers the component's own extent)
         c["bw"], c["bh"] = mcux * c["h"], mcuy * c["v"]
-        c["coef"] = np.zeros((c["bh"], c["bw"], 64), np.int64)
+        c["coef"] = [0] * (c["bh"] * c["bw"] * 64)  # flat (block row, block, natural order)
         # extent of a single-component scan (T.81 A.2.2)
         c["cw"] = -(-(-(-frame["w"] * c["h"] // hmax)) // 8)
         c["ch"] = -(-(-(-frame["h"] * c["v"] // vmax)) // 8)
@@ -243,23 +271,24 @@ def _decode_coefficients(data, frame, scans):
                 eobrun[0] = 0
             for k, by, bx in unit:
                 c, dt, at = sel[k]
-                blk = c["coef"][by, bx]
+                coef = c["coef"]
+                b0 = (by * c["bw"] + bx) * 64
                 if frame["progressive"]:
                     if ss == 0:
                         if ah == 0:  # DC first scan: the difference, scaled by 2^Al (G.1.2.1)
                             s = bits.decode(dt)
                             pred[k] += _extend(bits.bits(s), s)
-                            blk[0] = pred[k] << al
+                            coef[b0] = pred[k] << al
                         elif bits.bit():  # DC refinement: one more bit
-                            blk[0] |= 1 << al
+                            coef[b0] |= 1 << al
                     elif ah == 0:
-                        _ac_first(bits, at, blk, ss, se, al, eobrun)
+                        _ac_first(bits, at, coef, b0, ss, se, al, eobrun)
                     else:
-                        _ac_refine(bits, at, blk, ss, se, al, eobrun)
+                        _ac_refine(bits, at, coef, b0, ss, se, al, eobrun)
                     continue
                 s = bits.decode(dt)
                 pred[k] += _extend(bits.bits(s), s)
-                blk[0] = pred[k]
+                coef[b0] = pred[k]
                 z = 1
                 while z < 64:
                     rs = bits.decode(at)
@@ -272,12 +301,15 @@ def _decode_coefficients(data, frame, scans):
                     z += r
                     if z > 63:
                         raise JpegError("coefficient index out of range")
-                    blk[ZIGZAG[z]] = _extend(bits.bits(s), s)
+                    v = bits.bits(s)
+                    coef[b0 + _ZZ[z]] = v if v >> (s - 1) else v - (1 << s) + 1
                     z += 1
+    for c in comps:
+        c["coef"] = np.array(c["coef"], np.int64).reshape(c["bh"], c["bw"], 64)
     return comps, hmax, vmax
 
 
-def _ac_first(bits, table, blk, ss, se, al, eobrun):
+def _ac_first(bits, table, coef, b0, ss, se, al, eobrun):
     """First AC scan of one block (T.81 G.1.2.2): run/size symbols scaled by
     2^Al, ZRL, and end-of-band runs that cover whole blocks."""
     if eobrun[0] > 0:
@@ -291,7 +323,7 @@ def _ac_first(bits, table, blk, ss, se, al, eobrun):
             k += r
             if k > se:
                 raise JpegError("coefficient index out of range")
-            blk[ZIGZAG[k]] = _extend(bits.bits(s), s) << al
+            coef[b0 + _ZZ[k]] = _extend(bits.bits(s), s) << al
             k += 1
         elif r == 15:
             k += 16
@@ -300,7 +332,7 @@ def _ac_first(bits, table, blk, ss, se, al, eobrun):
             return
 
 
-def _ac_refine(bits, table, blk, ss, se, al, eobrun):
+def _ac_refine(bits, table, coef, b0, ss, se, al, eobrun):
     """AC refinement scan of one block (T.81 G.1.2.3): a correction bit for
     every coefficient already non-zero, new coefficients of magnitude 2^Al
     placed after runs of zero-history coefficients, and end-of-band runs
@@ -319,23 +351,23 @@ def _ac_refine(bits, table, blk, ss, se, al, eobrun):
                 eobrun[0] = (1 << r) + (bits.bits(r) if r else 0)
                 break
             while k <= se:
-                z = ZIGZAG[k]
-                if blk[z] != 0:
-                    if bits.bit() and (int(blk[z]) & p1) == 0:
-                        blk[z] += p1 if blk[z] >= 0 else m1
+                z = b0 + _ZZ[k]
+                if coef[z] != 0:
+                    if bits.bit() and (coef[z] & p1) == 0:
+                        coef[z] += p1 if coef[z] >= 0 else m1
                 else:
                     r -= 1
                     if r < 0:
                         break
                 k += 1
             if s and k <= se:
-                blk[ZIGZAG[k]] = s
+                coef[b0 + _ZZ[k]] = s
             k += 1
     if eobrun[0] > 0:
         while k <= se:
-            z = ZIGZAG[k]
-            if blk[z] != 0 and bits.bit() and (int(blk[z]) & p1) == 0:
-                blk[z] += p1 if blk[z] >= 0 else m1
+            z = b0 + _ZZ[k]
+            if coef[z] != 0 and bits.bit() and (coef[z] & p1) == 0:
+                coef[z] += p1 if coef[z] >= 0 else m1
             k += 1
         eobrun[0] -= 1
 
@@ -345,7 +377,7 @@ def _idct_plane(c, q):
     qn = np.zeros(64, np.int64)
     qn[ZIGZAG] = q
     f = (c["coef"] * qn).reshape(c["bh"], c["bw"], 8, 8).astype(np.float64)
-    px = np.einsum("ux,abuv,vy->abxy", _C, f, _C) + 128.0
+    px = np.matmul(np.matmul(_C.T, f), _C) + 128.0  # per block: C^T F C
     px = np.clip(np.floor(px + 0.5), 0, 255)
     return px.transpose(0, 2, 1, 3).reshape(c["bh"] * 8, c["bw"] * 8)
 
