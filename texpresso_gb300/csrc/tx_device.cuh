@@ -217,11 +217,32 @@ __device__ __forceinline__ uint2 encode_bc2_alpha(const uint32_t (&px)[16], uint
 // codebooks.
 
 // prmt.b32 in its generic mode: 4-bit selectors, bit 3 replicates the
-// selected byte's sign bit.
-__device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+// selected byte's sign bit.  (The host form lets the codebook builders below
+// be checked on the CPU.)
+__host__ __device__ __forceinline__ uint32_t prmt(uint32_t a, uint32_t b, uint32_t sel) {
+#ifdef __CUDA_ARCH__
     uint32_t d;
     asm("prmt.b32 %0, %1, %2, %3;" : "=r"(d) : "r"(a), "r"(b), "r"(sel));
     return d;
+#else
+    const uint64_t src = (uint64_t)a | ((uint64_t)b << 32);
+    uint32_t d = 0;
+    for (int k = 0; k < 4; ++k) {
+        const uint32_t s = (sel >> (4 * k)) & 0xFu;
+        uint32_t byte = (uint32_t)(src >> (8 * (s & 7u))) & 0xFFu;
+        if (s & 8u) byte = (byte & 0x80u) ? 0xFFu : 0x00u;
+        d |= byte << (8 * k);
+    }
+    return d;
+#endif
+}
+
+__host__ __device__ __forceinline__ int popc32(uint32_t x) {
+#ifdef __CUDA_ARCH__
+    return __popc(x);
+#else
+    return __builtin_popcount(x);
+#endif
 }
 
 // Lane-wise minimum / maximum of two pairs of unsigned 16-bit values.
@@ -237,7 +258,7 @@ __device__ __forceinline__ uint32_t max_u16x2(uint32_t a, uint32_t b) {
 }
 
 // 0xFF in every byte where x >= t (unsigned), else 0x00.
-__device__ __forceinline__ uint32_t bytes_ge(uint32_t x, uint32_t t) {
+__host__ __device__ __forceinline__ uint32_t bytes_ge(uint32_t x, uint32_t t) {
     const uint32_t H = 0x80808080u;
     const uint32_t g = (x | H) - (t & ~H);         // top bit: low 7 bits of x >= those of t
     const uint32_t m = (x & ~t) | (~(x ^ t) & g);  // top bit: x >= t
@@ -251,7 +272,7 @@ struct AlphaBook {
 };
 
 // 0xFF in every byte where x == y, else 0x00.
-__device__ __forceinline__ uint32_t bytes_eq(uint32_t x, uint32_t y) {
+__host__ __device__ __forceinline__ uint32_t bytes_eq(uint32_t x, uint32_t y) {
     const uint32_t H = 0x80808080u, d = x ^ y;
     return prmt(~(((d | H) - 0x01010101u) | d) & H, 0u, 0xBA98u);
 }
@@ -267,12 +288,12 @@ __device__ __forceinline__ uint32_t bytes_eq(uint32_t x, uint32_t y) {
 // are distinct otherwise, so merges never chain).  Thresholds between
 // neighbours (a, b) are (a + b + 2 - [ib < ia]) / 2 capped at 255: the
 // rounded-up byte average, plus one when a + b is even and ib > ia.
-__device__ __forceinline__ AlphaBook make_book7(uint32_t min5, uint32_t max5, const uint32_t (&c)[8]) {
+__host__ __device__ __forceinline__ AlphaBook make_book7(uint32_t min5, uint32_t max5, const uint32_t (&c)[8]) {
     const uint32_t A = c[2] | c[3] << 8 | c[4] << 16 | c[5] << 24;
     const uint32_t B6 = c[6] | c[7] << 8 | 0xFFFF0000u;  // padding bytes never count as below
     const uint32_t n5 = min5 * 0x01010101u, x5 = max5 * 0x01010101u;
-    const uint32_t p0 = (uint32_t)(__popc(~bytes_ge(A, n5)) + __popc(~bytes_ge(B6, n5))) >> 3;
-    const uint32_t p1 = ((uint32_t)(__popc(~bytes_ge(A, x5)) + __popc(~bytes_ge(B6, x5))) >> 3) + 1u;
+    const uint32_t p0 = (uint32_t)(popc32(~bytes_ge(A, n5)) + popc32(~bytes_ge(B6, n5))) >> 3;
+    const uint32_t p1 = ((uint32_t)(popc32(~bytes_ge(A, x5)) + popc32(~bytes_ge(B6, x5))) >> 3) + 1u;
     uint32_t sel = 0x76543210u - (0x11111111u << (4 * p0 + 4)) - (p1 < 7u ? 0x11111111u << (4 * p1 + 4) : 0u);
     sel = (sel & ~(0xFu << (4 * p0))) | (6u << (4 * p0));
     sel = (sel & ~(0xFu << (4 * p1))) | (7u << (4 * p1));
@@ -314,7 +335,7 @@ __device__ __forceinline__ AlphaBook make_book7(uint32_t min5, uint32_t max5, co
 // thresholds follow from the rule above with the index comparisons known; a
 // min5 of 0 gets threshold 0 (index 0 always beats index 6), and a max5 of 255
 // makes the last position index 1 again (the merge of equal values).
-__device__ __forceinline__ AlphaBook make_book5(uint32_t min5, uint32_t max5, const uint32_t (&c)[8]) {
+__host__ __device__ __forceinline__ AlphaBook make_book5(uint32_t min5, uint32_t max5, const uint32_t (&c)[8]) {
     AlphaBook bk;
     const uint32_t t[7] = {(min5 + 1u) >> 1,          (min5 + c[2] + 2u) >> 1, (c[2] + c[3] + 2u) >> 1,
                            (c[3] + c[4] + 2u) >> 1,   (c[4] + c[5] + 2u) >> 1, (c[5] + max5 + 1u) >> 1,
@@ -352,7 +373,7 @@ __device__ __forceinline__ int fit_book(const uint32_t (&x)[4], const uint32_t (
 }
 
 // fix_range (alpha.rs:70-77); min <= max on entry.
-__device__ __forceinline__ void fix_range(int &mn, int &mx, int steps) {
+__host__ __device__ __forceinline__ void fix_range(int &mn, int &mx, int steps) {
     if (mx - mn < steps) mx = min(mn + steps, 255);
     if (mx - mn < steps) mn = max(mx - steps, 0);
 }
