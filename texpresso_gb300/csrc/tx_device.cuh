@@ -62,14 +62,22 @@ inline void set_blocks_wide(SrcDesc &s, uint32_t bw) {
 }
 
 // Block column and row of block b.
-__device__ __forceinline__ void block_coords(const SrcDesc &s, size_t b, uint32_t &bx, uint32_t &by) {
+__host__ __device__ __forceinline__ uint32_t umulhi32(uint32_t a, uint32_t b) {
+#ifdef __CUDA_ARCH__
+    return __umulhi(a, b);
+#else
+    return (uint32_t)(((uint64_t)a * b) >> 32);
+#endif
+}
+
+__host__ __device__ __forceinline__ void block_coords(const SrcDesc &s, size_t b, uint32_t &bx, uint32_t &by) {
     if (b <= 0xFFFFFFFFull) {
         const uint32_t n = (uint32_t)b;
         uint32_t q;
         if (s.bw_flags & 2u) {
             q = n >> s.bw_shift;
         } else {
-            const uint32_t t = __umulhi(n, s.bw_magic);
+            const uint32_t t = umulhi32(n, s.bw_magic);
             q = (s.bw_flags & 1u) ? ((((n - t) >> 1) + t) >> s.bw_shift) : (t >> s.bw_shift);
         }
         by = q;
