@@ -14,14 +14,20 @@ no benchmark inputs.
   e2e     the same metric through the drop-in C-ABI call tx_compress with
           pinned host buffers: host->device copy of the RGBA8 input, kernel,
           device->host copy of the blocks, every step.
-  roofline  FP32-issue roofline of the ClusterFit kernel (algorithmic FP32
-          operations = reference candidate evaluations x ops per candidate;
-          the kernel skips, exactly, the candidates whose error lower bound
-          exceeds an error already reached, so this is a reference-equivalent
-          rate) plus the HBM roofline of the same launch (80 B per block) and
-          the issue-slot view (warp instructions per launch from the committed
-          ncu capture / the live launch time, against one warp instruction per
-          SM sub-partition per clock).
+  roofline  the ClusterFit kernel is bound by instruction issue (neither
+          HBM nor tensor cores): warp instructions per launch from an ncu
+          capture of the same kernel sources (profiles/counters.txt, checked
+          by a digest of the sources; null with the reason when stale) over
+          the live launch time, against one warp instruction per SM
+          sub-partition per clock; with the FP32 (FMA) pipe utilisation of
+          that capture.  roofline_hbm is the same launch against HBM (80 B
+          per block); reference_equivalent_fp32 counts the reference's
+          candidate evaluations x FP32 ops per candidate (the kernel skips,
+          exactly, candidates whose error bound excludes them).
+  parity  every output buffer the timed graph wrote, and the e2e output,
+          compared block by block with the oracle (identical fraction, ties,
+          non-ties); the run fails on a non-tie.  Every extra case carries
+          the same record.
   cpu_baseline  the CPU oracle (a C restatement of the reference's block
           path) on all host cores, one block row per task as rayon does.
   extra   the other formats / algorithms of the benchmark configurations,
@@ -169,18 +175,61 @@ class Clocks:
                 "reasons": sorted(reasons)}
 
 
-def dram_traffic():
-    """Per-launch DRAM bytes from the committed ncu summaries (profiles/dram_traffic.txt)."""
-    out = {}
-    try:
-        with open(os.path.join(ROOT, "profiles", "dram_traffic.txt")) as f:
-            for line in f:
-                line = line.split("#")[0].split()
-                if len(line) >= 2:
-                    out[line[0]] = int(line[1])
-    except (OSError, ValueError):
-        pass
-    return out
+def source_digest():
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("tx_build", os.path.join(ROOT, "texpresso_gb300", "build.py"))
+    mod = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mod)
+    return mod.source_digest()
+
+
+class Counters:
+    """Per-launch ncu counters of the benchmark's kernels (profiles/counters.txt:
+    `case.metric value digest` per line).  A count is used only when its digest
+    equals the digest of the kernel sources being run: a count captured from
+    another build would divide that build's instructions by this build's time."""
+
+    def __init__(self):
+        self.digest = source_digest()
+        self.rows, self.stale = {}, set()
+        try:
+            with open(os.path.join(ROOT, "profiles", "counters.txt")) as f:
+                for line in f:
+                    parts = line.split("#")[0].split()
+                    if len(parts) >= 3:
+                        if parts[2] == self.digest:
+                            self.rows[parts[0]] = float(parts[1])
+                        else:
+                            self.stale.add(parts[0].split(".")[0])
+        except (OSError, ValueError):
+            pass
+
+    def get(self, case, metric):
+        return self.rows.get("%s.%s" % (case, metric))
+
+    def why_missing(self, case):
+        if case in self.stale:
+            return "profiles/counters.txt holds %s counts from other kernel sources (digest %s expected)" % (
+                case, self.digest)
+        return "no ncu capture of %s in profiles/counters.txt" % case
+
+
+def issue_view(ctr, case, ms_step, sm_mhz):
+    """Executed issue-slot roofline of one launch: warp instructions per launch
+    (ncu, same sources) / this run's launch time, against one warp instruction
+    per SM sub-partition per clock (152 SMs x 4)."""
+    inst = ctr.get(case, "inst")
+    if inst is None:
+        return None, ctr.why_missing(case)
+    peak = 152 * 4 * sm_mhz * 1e6 / 1e9
+    got = inst / (ms_step * 1e-3) / 1e9
+    rec = {"bound": "issue", "achieved": round(got, 1), "peak": round(peak, 1), "unit": "Ginst/s",
+           "frac": round(got / peak, 4), "inst_per_launch": int(inst)}
+    for k in ("fma_pct", "alu_pct", "issue_pct", "dram"):
+        v = ctr.get(case, k)
+        if v is not None:
+            rec["ncu_" + k] = v
+    return rec, None
 
 
 def peaks():
@@ -241,6 +290,10 @@ class DeviceRun:
     def output(self, i=0):
         return self.dst[i].cpu().numpy()
 
+    def outputs(self, launched):
+        """Every output buffer the launches so far have written."""
+        return [d.cpu().numpy() for d in self.dst[:min(len(self.dst), launched)]]
+
 
 def e2e_time(torch, tx, fmt, img, params, steps, warmup):
     """tx_compress (host buffers, synchronous) on pinned memory, wall clock."""
@@ -256,7 +309,7 @@ def e2e_time(torch, tx, fmt, img, params, steps, warmup):
     for _ in range(steps):
         f.compress(srcn, w, h, params, dstn)
     dt = time.perf_counter() - t0
-    return dt * 1e3, src.numel(), dst.numel()
+    return dt * 1e3, src.numel(), dst.numel(), dstn.copy()
 
 
 # ---------------------------------------------------------------------------
@@ -285,6 +338,53 @@ def cpu_rate(oracle, fmt, img, params, seconds, nthreads=0):
 
 
 # ---------------------------------------------------------------------------
+# oracle parity of the timed outputs (the oracle is the checker here)
+
+def colour_error(oracle, fmt, enc, src16, mask, weights):
+    """Sum over valid, non-transparent pixels of sum_c w_c (decoded - source)^2
+    with the linear channel weights ClusterFit applies (cluster.rs:219)."""
+    dec = oracle.decompress_block(fmt, enc).reshape(16, 4).astype(np.float64)
+    s = src16.reshape(16, 4).astype(np.float64)
+    e = 0.0
+    for p in range(16):
+        if (mask >> p) & 1 and not (fmt == 0 and s[p, 3] < 128):
+            e += sum(weights[c] * (dec[p, c] - s[p, c]) ** 2 for c in range(3))
+    return e
+
+
+def oracle_parity(oracle, fmt, rgba, alg, weights, aw, outputs):
+    """Compare every output buffer of a timed run with the oracle's compress of
+    the same input, block by block.  A differing ClusterFit block counts as a
+    tie when its colour half decodes to a squared error within 1e-6 relative
+    of the oracle's and its alpha half is identical; anything else is a
+    non-tie (SingleColourFit, RangeFit and the alpha paths must be
+    bit-identical)."""
+    from texpresso_gb300 import workloads
+    h, w = rgba.shape[:2]
+    ref = oracle.compress(fmt, rgba, w, h, oracle.make_params(alg, tuple(weights), aw))
+    bs = 8 if fmt in (0, 3) else 16
+    r = ref.reshape(-1, bs)
+    n = r.shape[0]
+    blocks = masks = None
+    rec = {"blocks": 0, "identical": 0, "ties": 0, "non_ties": 0}
+    for got in outputs:
+        g = np.asarray(got).reshape(-1, bs)[:n]
+        diff = np.flatnonzero(np.any(g != r, axis=1))
+        rec["blocks"] += n
+        rec["identical"] += n - diff.size
+        for b in diff:
+            tie = False
+            if alg != 0 and fmt < 3 and (fmt == 0 or np.array_equal(g[b, :8], r[b, :8])):
+                if blocks is None:
+                    blocks, masks = workloads.image_to_blocks(rgba)
+                eg = colour_error(oracle, fmt, g[b], blocks[b], int(masks[b]), weights)
+                er = colour_error(oracle, fmt, r[b], blocks[b], int(masks[b]), weights)
+                tie = abs(eg - er) <= 1e-6 * max(er, 1e-12)
+            rec["ties" if tie else "non_ties"] += 1
+    rec["identical_fraction"] = round(rec["identical"] / max(1, rec["blocks"]), 6)
+    rec["buffers"] = len(outputs)
+    return rec
+
 
 def headline_image(size, seed=0):
     from texpresso_gb300 import workloads
@@ -380,13 +480,27 @@ def run_ours(args):
 
     # end to end through the drop-in host call
     e2e_steps = max(3, min(args.steps, 50))
-    e2e_ms, h2d, d2h = e2e_time(torch, tx, 2, img, params, e2e_steps, max(3, args.warmup))
+    e2e_ms, h2d, d2h, e2e_out = e2e_time(torch, tx, 2, img, params, e2e_steps, max(3, args.warmup))
     e2e_ms = replicas.max_over_ranks(e2e_ms, dev)
     e2e_value = world_size * e2e_steps * nb / (e2e_ms * 1e-3) / 1e6
 
     ops = cluster_ops(img, 2)
     achieved_tops = ops / (ms_step * 1e-3) / 1e12
     hbm_achieved = BYTES_PER_BLOCK[2] * nb / (ms_step * 1e-3) / 1e9
+    ctr = Counters()
+    issue, issue_missing = issue_view(ctr, "c1_bc3_cluster", ms_step, sm_max_mhz)
+    traffic = ctr.get("c1_bc3_cluster", "dram")
+    if issue is not None:
+        roofline = dict(issue)
+        roofline["traffic"] = int(traffic) if traffic is not None else None
+        roofline["kernel"] = "k_cluster<BC3,32,1>"
+        roofline["basis"] = ("warp instructions per launch (ncu smsp__inst_executed.sum, profiles/counters.txt, "
+                             "digest %s = these sources) / this run's launch time; peak 152 SMs x 4 "
+                             "sub-partitions x 1 warp instruction per clock at %.0f MHz; ncu_fma_pct = FP32 "
+                             "(FMA) pipe issue utilisation" % (ctr.digest, sm_max_mhz))
+    else:
+        roofline = {"bound": "issue", "achieved": None, "peak": round(152 * 4 * sm_max_mhz * 1e6 / 1e9, 1),
+                    "unit": "Ginst/s", "frac": None, "traffic": None, "missing": issue_missing}
     line = {
         "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms_step, 5), "higher_is_better": True, "scaling": "weak",
@@ -395,34 +509,22 @@ def run_ours(args):
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
                 "api": "tx_compress (C ABI, pinned host buffers)", "steps": e2e_steps},
         "gpu_launches": launches,
-        "roofline": {"bound": "fp32", "achieved": round(achieved_tops, 3), "peak": round(fp32_peak_tops, 2),
-                     "unit": "TFLOP/s", "frac": round(achieved_tops / fp32_peak_tops, 4), "traffic": None,
-                     "work": "%d FP32 ops per launch = the reference's candidate evaluations x %d (compress4); "
-                             "the kernel bounds every candidate's error from below and evaluates the exact error "
-                             "only where the bound does not exclude it (about 4 %%), so this is the "
-                             "reference-equivalent rate, not the FP32 rate executed (issue-slot use: "
-                             "profiles/k_cluster_bc3_2048.md)" % (ops, OPS_CAND4),
-                     "peak_basis": "nominal: 152 SMs x 128 FP32 lanes x %.0f MHz (sm_max_mhz)" % sm_max_mhz},
+        "roofline": roofline,
         "roofline_hbm": {"bound": "hbm", "achieved": round(hbm_achieved, 1), "peak": hbm_peak, "unit": "GB/s",
-                         "frac": round(hbm_achieved / hbm_peak, 4), "traffic": None,
+                         "frac": round(hbm_achieved / hbm_peak, 4),
+                         "traffic": int(traffic) if traffic is not None else None,
                          "basis": "80 B per block (64 B RGBA8 + 16 B BC3) x %d blocks; peak %s" % (nb, peak_kind)},
+        "reference_equivalent_fp32": {
+            "achieved": round(achieved_tops, 3), "unit": "TFLOP/s", "nominal_peak": round(fp32_peak_tops, 2),
+            "ratio_to_nominal": round(achieved_tops / fp32_peak_tops, 4),
+            "work": "%d FP32 ops per launch = the reference's candidate evaluations x %d (compress4); the kernel "
+                    "bounds every candidate's error from below and evaluates the exact error only where the bound "
+                    "does not exclude it, so this is how fast the reference's work gets done, not FP32 executed"
+                    % (ops, OPS_CAND4)},
         "clocks": clk,
     }
-    inst = dram_traffic().get("bc3_cluster_%d_inst" % size)
-    if inst is not None:
-        issue_peak = 152 * 4 * sm_max_mhz * 1e6 / 1e9
-        issue_achieved = inst / (ms_step * 1e-3) / 1e9
-        line["roofline_issue"] = {
-            "bound": "issue", "achieved": round(issue_achieved, 1), "peak": round(issue_peak, 1), "unit": "Ginst/s",
-            "frac": round(issue_achieved / issue_peak, 4),
-            "basis": "%d warp instructions per launch (smsp__inst_executed.sum, profiles/k_cluster_bc3_2048.md) / "
-                     "this run's launch time; peak 152 SMs x 4 sub-partitions x 1 warp instruction per clock at "
-                     "%.0f MHz" % (inst, sm_max_mhz)}
-    traffic = dram_traffic().get("bc3_cluster_%d" % size)
-    if traffic is not None:
-        line["roofline"]["traffic"] = traffic
-        line["roofline_hbm"]["traffic"] = traffic
 
+    summary = {}
     if rank == 0 and world_size == 1:
         from oracle import oracle
         cores = oracle.online_cores()
@@ -431,15 +533,44 @@ def run_ours(args):
                                 "sample": "%d blocks of the same texture in %.1f s, %d threads, one block row per "
                                           "task (C oracle, -O3 -ffp-contract=off)" % (cpu_blocks, cpu_dt, cores)}
         line["speedup_vs_cpu"] = {"value": round(value / cpu_v, 1), "e2e": round(e2e_value / cpu_v, 1)}
+        # the timed outputs (every HBM copy the graph wrote) and the e2e output against the oracle
+        par = oracle_parity(oracle, 2, img, 1, tx.COLOUR_WEIGHTS_PERCEPTUAL, False,
+                            run.outputs(max(args.steps, args.warmup)) + [e2e_out])
+        line["parity"] = par
+        summary["C1 BC3 ClusterFit (headline)"] = {
+            "mblocks_s": round(value, 1), "e2e": round(e2e_value, 1), "cpu": round(cpu_v, 3),
+            "issue_frac": roofline.get("frac"), "identical": par["identical_fraction"], "ties": par["ties"],
+            "non_ties": par["non_ties"]}
         if not args.no_extra:
-            line["extra"] = extras(torch, tx, oracle, args, hbm_peak, fp32_peak_tops)
+            line["extra"] = extras(torch, tx, oracle, args, hbm_peak, fp32_peak_tops, ctr, sm_max_mhz)
+            for label, rec in line["extra"].items():
+                summary[label] = {k: v for k, v in (
+                    ("mblocks_s", round(rec["mblocks_s"], 1)), ("cpu", rec.get("cpu_mblocks_s")),
+                    ("hbm_frac", rec["hbm"]["frac"]), ("issue_frac", (rec.get("issue") or {}).get("frac")),
+                    ("identical", rec["parity"]["identical_fraction"]), ("ties", rec["parity"]["ties"]),
+                    ("non_ties", rec["parity"]["non_ties"])) if v is not None}
             line["batched"] = batched(torch, tx, args)
+            summary["C3 batched"] = {k: line["batched"][k] for k in (
+                "batch_mblocks_s", "gain_vs_per_call_eager", "gain_vs_per_call_graph", "identical_to_per_call")}
+            summary["C3 batched"]["tuning"] = line["batched"]["tuning"]
             line["serving"] = serving(torch, tx, args)
+            summary["C4 serving"] = {r: {"gain": v["throughput_gain"], "p50": [v["served"]["p50_ms"],
+                                                                              v["plain"]["p50_ms"]],
+                                         "p99": [v["served"]["p99_ms"], v["plain"]["p99_ms"]],
+                                         "same": v["identical_outputs"]}
+                                     for r, v in line["serving"]["rates"].items()}
+    non_ties = sum(v.get("non_ties", 0) for v in summary.values() if isinstance(v, dict))
+    if summary:
+        # last key of the line, so that a reader of the line's tail sees every case
+        line["summary"] = summary
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world_size > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+    if non_ties:
+        print("bench: %d timed blocks differ from the oracle beyond a tie" % non_ties, file=sys.stderr)
+        return 1
     return 0
 
 
@@ -488,12 +619,8 @@ def extra_cases(tx, names=None):
     return out
 
 
-# warp instructions per launch of a case's kernel, from profiles/dram_traffic.txt
-CASE_INST = {"c1_bc3_range": "bc3_range_2048_inst", "c2_bc4_r8": "bc4_r8_4096_inst",
-             "bc1_iter_cluster": "bc1_iter_2048_inst", "c1_bc3_cluster": "bc3_cluster_2048_inst"}
-
-
-def time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak, inst=None):
+def time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak, ctr=None, key=None, sm_mhz=2070.0,
+              keep_outputs=False):
     from texpresso_gb300 import workloads
     r = DeviceRun(torch, tx, fmt, [img], p, channels=ch)
     ms, launches = r.time(steps, 3)
@@ -504,35 +631,42 @@ def time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak, inst=
     bpb = BYTES_PER_BLOCK_NATIVE[fmt] if ch in (1, 2) else BYTES_PER_BLOCK[fmt]
     gbs = bpb * r.nblocks / (ms_step * 1e-3) / 1e9
     rec["hbm"] = {"achieved_gbs": round(gbs, 1), "frac": round(gbs / hbm_peak, 4), "bytes_per_block": bpb}
+    if ctr is not None and key is not None:
+        t = ctr.get(key, "dram")
+        if t is not None:
+            rec["hbm"]["traffic"] = int(t)
     if alg == 1 and fmt < 3:
         rgba_img = img if ch == 4 else workloads.expand_to_rgba(img)
         ops = cluster_ops(rgba_img, fmt)
         tops = ops / (ms_step * 1e-3) / 1e12
-        rec["fp32"] = {"achieved_tops": round(tops, 3), "frac": round(tops / fp32_peak, 4)}
-    if inst:
-        # these kernels are bound by instruction issue, not HBM: the executed view
-        issue_peak = fp32_peak * 1e3 / 32.0  # Ginst/s: one warp instruction per scheduler and clock
-        gi = inst / (ms_step * 1e-3) / 1e9
-        rec["issue"] = {"achieved_ginst_s": round(gi, 1), "frac": round(gi / issue_peak, 4),
-                        "inst_per_launch": inst}
+        rec["reference_equivalent_fp32"] = {"achieved_tops": round(tops, 3),
+                                            "ratio_to_nominal": round(tops / fp32_peak, 4)}
+    if ctr is not None and key is not None:
+        issue, missing = issue_view(ctr, key, ms_step, sm_mhz)
+        rec["issue"] = issue if issue is not None else {"frac": None, "missing": missing}
+    outs = r.outputs(max(steps, 3)) if keep_outputs else None
     del r
     torch.cuda.empty_cache()
-    return rec
+    return (rec, outs) if keep_outputs else rec
 
 
-def extras(torch, tx, oracle, args, hbm_peak, fp32_peak):
-    """Other format/algorithm configurations, each beside the CPU oracle."""
+def extras(torch, tx, oracle, args, hbm_peak, fp32_peak, ctr, sm_mhz):
+    """Other format/algorithm configurations, each beside the CPU oracle and
+    checked block by block against it."""
     from texpresso_gb300 import workloads
     out = {}
     steps = max(20, min(200, args.steps))
     for key, label, fmt, img, p, alg, ch in extra_cases(tx):
-        rec = time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak,
-                        dram_traffic().get(CASE_INST.get(key, ""), None))
+        rec, outs = time_case(torch, tx, fmt, img, p, alg, ch, steps, hbm_peak, fp32_peak, ctr, key, sm_mhz,
+                              keep_outputs=True)
         rgba_img = img if ch == 4 else workloads.expand_to_rgba(img)
         op = oracle.make_params(alg, tuple(p.weights), p.weigh_colour_by_alpha)
         cv, _, _ = cpu_rate(oracle, fmt, rgba_img, op, 2.5)
         rec["cpu_mblocks_s"] = round(cv, 4)
         rec["speedup_vs_cpu"] = round(rec["mblocks_s"] / cv, 1)
+        # every output buffer the timed launches wrote (two suffice: all hold the same input)
+        rec["parity"] = oracle_parity(oracle, fmt, rgba_img, alg, tuple(p.weights), p.weigh_colour_by_alpha,
+                                      outs[:2])
         out[label] = rec
     return out
 
@@ -728,8 +862,8 @@ def run_case(args):
     hbm_peak, sm_max_mhz, _ = peaks()
     fp32_peak = 152 * 128 * sm_max_mhz * 1e6 / 1e12
     (key, label, fmt, img, p, alg, ch), = extra_cases(tx, [args.case])
-    rec = time_case(torch, tx, fmt, img, p, alg, ch, args.steps, hbm_peak, fp32_peak,
-                    dram_traffic().get(CASE_INST.get(key, ""), None))
+    rec = time_case(torch, tx, fmt, img, p, alg, ch, args.steps, hbm_peak, fp32_peak, Counters(), key,
+                    sm_max_mhz)
     rec["case"] = key
     rec["label"] = label
     print(json.dumps(rec), flush=True)

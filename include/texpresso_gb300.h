@@ -165,7 +165,8 @@ TX_API void tx_batch_default_tuning(tx_batch_tuning *tuning);
 
 /* Validate the items and build the plan (allocates device memory for the
  * item table, the work queues and two counters).  Items are read at launch
- * time, so their buffers must stay valid while the plan is launched. */
+ * time, so their buffers must stay valid while the plan is launched.  A level
+ * of more than 2^31 - 1 blocks returns TX_ERR_INVALID_ARGUMENT. */
 TX_API int tx_batch_create(const tx_batch_item *items, size_t nitems, const tx_batch_tuning *tuning,
                            tx_batch **batch);
 
@@ -190,12 +191,16 @@ TX_API void tx_batch_destroy(tx_batch *batch);
  * callers that must not have a library allocate device memory -- engines that
  * reserve the whole memory budget up front and hand it out through their own
  * allocator, or per-frame loops that cannot take the implicit synchronisation
- * of an allocation or free.  Compresses up to 256 texture levels exactly as
- * tx_batch_create + tx_batch_launch would, but keeps the work queue in a
- * fixed 1 MiB array of device memory that the library declares statically
- * (every GPU that loads the library holds it until the process exits), so the
- * call itself allocates nothing.  The caller passes inputs and outputs as in
- * tx_batch_item.  More than 256 items returns TX_ERR_INVALID_ARGUMENT.
+ * of an allocation or free.  Compresses up to 256 texture levels to the same
+ * output bytes as tx_batch_create + tx_batch_launch (and tx_compress_device),
+ * but keeps the work queue in a fixed 1 MiB array of device memory that the
+ * library declares statically (every GPU that loads the library holds it
+ * until the process exits), so the call itself allocates nothing.  When the
+ * default work units would overflow that array, the units grow (more blocks
+ * per unit) until the queue fits, so the scheduling differs from
+ * tx_batch_launch while the bytes do not.  The caller passes inputs and
+ * outputs as in tx_batch_item.  More than 256 items, or a level of more than
+ * 2^31 - 1 blocks, returns TX_ERR_INVALID_ARGUMENT.
  * Stream-ordered.  The first call on each device does a one-time set-up with
  * that device current (it looks up the array's device address); make that
  * first call before any stream capture.  All calls share the array, so calls

@@ -124,3 +124,40 @@ def test_native_channel_items(tx, cuda, oracle):
     for (fmt, ch), o in zip(((3, 1), (4, 2), (3, 4), (4, 4)), outs):
         assert np.array_equal(o.cpu().numpy(), oracle.compress(fmt, rgba, 70, 45, oracle.make_params())), (fmt, ch)
     b.close()
+
+
+def test_config3_textures_match_oracle(tx, cuda, oracle):
+    """Thirty textures of the benchmark's own 1,000-texture batch
+    (batch_specs(1000, seed=0), the same content generator): the largest of
+    every format x algorithm class (up to 3880x2918) and 21 others drawn at
+    random, every mip level compressed by one batch launch and compared with
+    the oracle's compress of that level (lib/src/lib.rs:287-335), bit for bit."""
+    from texpresso_gb300.texture_set import TextureSet
+    specs = workloads.batch_specs(1000, seed=0)
+    largest = {}
+    for i, s in enumerate(specs):
+        k = (s["format"], s["algorithm"])
+        if k not in largest or s["width"] * s["height"] > specs[largest[k]]["width"] * specs[largest[k]]["height"]:
+            largest[k] = i
+    assert len(largest) == 9
+    rest = [i for i in range(len(specs)) if i not in set(largest.values())]
+    pick = sorted(set(largest.values()) | set(np.random.default_rng(1).choice(rest, 21, replace=False).tolist()))
+    chosen = [specs[i] for i in pick]
+    ts = TextureSet(chosen, device="cuda")
+    st = cuda.cuda.current_stream().cuda_stream
+    b = tx.Batch(ts.items())
+    b.launch(st)
+    cuda.cuda.synchronize()
+    got = ts.snapshot()
+    b.close()
+    levels = blocks = 0
+    for i, s in enumerate(chosen):
+        op = oracle.make_params(s["algorithm"], (0.2126, 0.7152, 0.0722), False)
+        for lvl, img in enumerate(l.cpu().numpy() for l in ts.levels[i]):
+            h, w = img.shape[:2]
+            ref = oracle.compress(s["format"], img, w, h, op)
+            assert np.array_equal(got[i][lvl], ref), "texture %d (%dx%d fmt %d alg %d) level %d differs" % (
+                pick[i], s["width"], s["height"], s["format"], s["algorithm"], lvl)
+            levels += 1
+            blocks += tx.num_blocks(w) * tx.num_blocks(h)
+    print("config-3 oracle check: %d textures, %d levels, %d blocks identical" % (len(chosen), levels, blocks))

@@ -71,6 +71,66 @@ def test_noalloc_matches_existing_entry_point_twice(tx, cuda):
         del srcs
 
 
+def _flat_blocks_texture(torch, width, height, seed, noisy_every=64):
+    """RGBA8 on the device: one random colour per 4x4 block (the single-colour
+    path), every `noisy_every`-th block a noisy ramp instead (full ClusterFit)."""
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    bw, bh = width // 4, height // 4
+    col = torch.randint(0, 256, (bh, bw, 4), generator=g, device="cuda", dtype=torch.uint8)
+    col[..., 3] = 255
+    img = col.repeat_interleave(4, 0).repeat_interleave(4, 1).contiguous()
+    noise = torch.randint(0, 256, (height, width, 3), generator=g, device="cuda", dtype=torch.uint8)
+    sel = torch.zeros((bh, bw), dtype=torch.bool, device="cuda")
+    sel.view(-1)[::noisy_every] = True
+    sel = sel.repeat_interleave(4, 0).repeat_interleave(4, 1)
+    img[..., :3] = torch.where(sel[..., None], noise, img[..., :3])
+    return img
+
+
+def test_noalloc_large_levels_grow_the_units(tx, cuda):
+    """Levels large enough that the default units overflow the fixed array:
+    the team units grow past 64 blocks (an 8.4 M-block BC1 ClusterFit level)
+    and the lane units past 64 blocks (8192x8192 BC4 R8 and BC5 RG8), with an
+    IterativeClusterFit level drained by the prefetching team kernel at the
+    grown unit size.  Bytes must still equal the per-level entry point's, on
+    two calls in a row."""
+    torch = cuda
+    launch = _noalloc(tx)
+    stream = torch.cuda.current_stream().cuda_stream
+    g = torch.Generator(device="cuda").manual_seed(5)
+    C = tx.Algorithm.ClusterFit
+    levels = [
+        (0, 16384, 8192, 4, tx.Params(algorithm=C), _flat_blocks_texture(torch, 16384, 8192, 1)),
+        (3, 8192, 8192, 1, tx.Params(),
+         torch.randint(0, 256, (8192, 8192, 1), generator=g, device="cuda", dtype=torch.uint8)),
+        (4, 8192, 8192, 2, tx.Params(),
+         torch.randint(0, 256, (8192, 8192, 2), generator=g, device="cuda", dtype=torch.uint8)),
+        (2, 1024, 1024, 4, tx.Params(algorithm=tx.Algorithm.IterativeClusterFit),
+         torch.from_numpy(workloads.ramp_texture(1024, 1024, seed=6, alpha="ramp")).cuda()),
+        (2, 516, 509, 4, tx.Params(algorithm=C, weigh_colour_by_alpha=True),
+         torch.from_numpy(workloads.ramp_texture(516, 509, seed=7, alpha="ramp")).cuda()),
+    ]
+    ref, items, outs = [], [], []
+    for fmt, w, h, ch, p, img in levels:
+        n_out = tx.Format(fmt).compressed_size(w, h)
+        r = torch.zeros(n_out, dtype=torch.uint8, device="cuda")
+        tx.compress_device(tx.Format(fmt), img.data_ptr(), w * ch, ch, w, h, p, r.data_ptr(), n_out, stream)
+        ref.append(r)
+        o = torch.zeros(n_out, dtype=torch.uint8, device="cuda")
+        outs.append(o)
+        items.append(tx.batch_item(fmt, img.data_ptr(), w * ch, w, h, p, o.data_ptr(), channels=ch))
+    arr = (tx.BatchItem * len(items))(*items)
+    for call in range(2):
+        for o in outs:
+            o.fill_(0xA5)
+        rc = launch(arr, len(items), stream)
+        assert rc == 0, tx.TexpressoError(rc, "tx_batch_launch_noalloc")
+        torch.cuda.synchronize()
+        for k, (o, r) in enumerate(zip(outs, ref)):
+            assert torch.equal(o, r), "call %d, level %d differs in %d bytes" % (
+                call, k, int((o != r).sum()))
+
+
 def test_noalloc_rejects_more_items_than_the_array_holds(tx, cuda):
     torch = cuda
     launch = _noalloc(tx)

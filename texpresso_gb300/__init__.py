@@ -33,7 +33,37 @@ if not os.path.exists(LIB_PATH):
         "texpresso_gb300: %s is missing; build it first with "
         "`python -c 'import __graft_entry__ as g; g.build()'` (needs nvcc)" % LIB_PATH)
 
-_lib = ctypes.CDLL(LIB_PATH)
+_SIGS = {}
+
+
+def _sig(name, what, value):
+    """Record a ctypes signature; applied when the library is first opened."""
+    _SIGS.setdefault(name, {})[what] = value
+    if _Lib.handle is not None:
+        setattr(getattr(_Lib.handle, name), what, value)
+
+
+class _Lib:
+    """The C library, opened on first use: importing the package (or its numpy
+    workload generators) maps nothing; the first call opens
+    libtexpresso_gb300.so and fails loudly if it cannot."""
+    handle = None
+
+    @staticmethod
+    def open():
+        if _Lib.handle is None:
+            h = ctypes.CDLL(LIB_PATH)
+            for fn, sig in _SIGS.items():
+                for what, value in sig.items():
+                    setattr(getattr(h, fn), what, value)
+            _Lib.handle = h
+        return _Lib.handle
+
+    def __getattr__(self, name):
+        return getattr(_Lib.open(), name)
+
+
+_lib = _Lib()
 
 TX_OK = 0
 STATUS = {
@@ -62,25 +92,25 @@ class _CParams(ctypes.Structure):
 _u8p = ctypes.POINTER(ctypes.c_uint8)
 _sz = ctypes.c_size_t
 _vp = ctypes.c_void_p
-_lib.tx_status_string.restype = ctypes.c_char_p
-_lib.tx_status_string.argtypes = [ctypes.c_int]
-_lib.tx_params_default.argtypes = [ctypes.POINTER(_CParams)]
-_lib.tx_num_blocks.restype = _sz
-_lib.tx_num_blocks.argtypes = [_sz]
-_lib.tx_block_size.restype = _sz
-_lib.tx_block_size.argtypes = [ctypes.c_int]
-_lib.tx_compressed_size.restype = _sz
-_lib.tx_compressed_size.argtypes = [ctypes.c_int, _sz, _sz]
-_lib.tx_compress.argtypes = [ctypes.c_int, _vp, _sz, _sz, _sz, ctypes.POINTER(_CParams), _vp, _sz]
-_lib.tx_compress_block_masked.argtypes = [ctypes.c_int, _vp, ctypes.c_uint32, ctypes.POINTER(_CParams), _vp, _sz]
-_lib.tx_compress_device.argtypes = [ctypes.c_int, _vp, _sz, ctypes.c_int, _sz, _sz, ctypes.POINTER(_CParams),
-                                    _vp, _sz, _vp]
-_lib.tx_compress_blocks_device.argtypes = [ctypes.c_int, _vp, _vp, _sz, ctypes.POINTER(_CParams), _vp, _vp]
-_lib.tx_decompress.argtypes = [ctypes.c_int, _vp, _sz, _sz, _sz, _vp, _sz]
-_lib.tx_decompress_block.argtypes = [ctypes.c_int, _vp, _sz, _vp]
-_lib.tx_decompress_device.argtypes = [ctypes.c_int, _vp, _sz, _sz, _sz, _vp, _sz, _vp]
-_lib.tx_last_cuda_error.restype = ctypes.c_int
-_lib.tx_kernel_launch_count.restype = ctypes.c_uint64
+_sig("tx_status_string", "restype", ctypes.c_char_p)
+_sig("tx_status_string", "argtypes", [ctypes.c_int])
+_sig("tx_params_default", "argtypes", [ctypes.POINTER(_CParams)])
+_sig("tx_num_blocks", "restype", _sz)
+_sig("tx_num_blocks", "argtypes", [_sz])
+_sig("tx_block_size", "restype", _sz)
+_sig("tx_block_size", "argtypes", [ctypes.c_int])
+_sig("tx_compressed_size", "restype", _sz)
+_sig("tx_compressed_size", "argtypes", [ctypes.c_int, _sz, _sz])
+_sig("tx_compress", "argtypes", [ctypes.c_int, _vp, _sz, _sz, _sz, ctypes.POINTER(_CParams), _vp, _sz])
+_sig("tx_compress_block_masked", "argtypes", [ctypes.c_int, _vp, ctypes.c_uint32, ctypes.POINTER(_CParams), _vp, _sz])
+_sig("tx_compress_device", "argtypes", [ctypes.c_int, _vp, _sz, ctypes.c_int, _sz, _sz, ctypes.POINTER(_CParams),
+                                        _vp, _sz, _vp])
+_sig("tx_compress_blocks_device", "argtypes", [ctypes.c_int, _vp, _vp, _sz, ctypes.POINTER(_CParams), _vp, _vp])
+_sig("tx_decompress", "argtypes", [ctypes.c_int, _vp, _sz, _sz, _sz, _vp, _sz])
+_sig("tx_decompress_block", "argtypes", [ctypes.c_int, _vp, _sz, _vp])
+_sig("tx_decompress_device", "argtypes", [ctypes.c_int, _vp, _sz, _sz, _sz, _vp, _sz, _vp])
+_sig("tx_last_cuda_error", "restype", ctypes.c_int)
+_sig("tx_kernel_launch_count", "restype", ctypes.c_uint64)
 
 
 def _check(rc, what):
@@ -213,7 +243,7 @@ def kernel_launch_count():
 
 def library():
     """The loaded ctypes library (for tests of the raw C ABI)."""
-    return _lib
+    return _Lib.open()
 
 
 # ---------------------------------------------------------------------------
@@ -241,18 +271,18 @@ class MipJob(ctypes.Structure):
                 ("channels", ctypes.c_int32), ("dst", _vp), ("dst_pitch", _sz)]
 
 
-_lib.tx_batch_default_tuning.argtypes = [ctypes.POINTER(BatchTuning)]
-_lib.tx_batch_create.argtypes = [ctypes.POINTER(BatchItem), _sz, ctypes.POINTER(BatchTuning), ctypes.POINTER(_vp)]
-_lib.tx_batch_launch.argtypes = [_vp, _vp]
-_lib.tx_batch_set_tuning.argtypes = [_vp, ctypes.POINTER(BatchTuning)]
-_lib.tx_batch_get_tuning.argtypes = [_vp, ctypes.POINTER(BatchTuning)]
-_lib.tx_batch_info.argtypes = [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_sz), ctypes.POINTER(_sz)]
-_lib.tx_batch_autotune.argtypes = [_vp, _vp, ctypes.c_int, ctypes.POINTER(BatchTuning)]
-_lib.tx_batch_destroy.argtypes = [_vp]
-_lib.tx_batch_destroy.restype = None
-_lib.tx_mip_count.restype = ctypes.c_uint32
-_lib.tx_mip_count.argtypes = [ctypes.c_uint32, ctypes.c_uint32]
-_lib.tx_mip_batch_device.argtypes = [ctypes.POINTER(MipJob), _sz, _vp]
+_sig("tx_batch_default_tuning", "argtypes", [ctypes.POINTER(BatchTuning)])
+_sig("tx_batch_create", "argtypes", [ctypes.POINTER(BatchItem), _sz, ctypes.POINTER(BatchTuning), ctypes.POINTER(_vp)])
+_sig("tx_batch_launch", "argtypes", [_vp, _vp])
+_sig("tx_batch_set_tuning", "argtypes", [_vp, ctypes.POINTER(BatchTuning)])
+_sig("tx_batch_get_tuning", "argtypes", [_vp, ctypes.POINTER(BatchTuning)])
+_sig("tx_batch_info", "argtypes", [_vp, ctypes.POINTER(_sz), ctypes.POINTER(_sz), ctypes.POINTER(_sz)])
+_sig("tx_batch_autotune", "argtypes", [_vp, _vp, ctypes.c_int, ctypes.POINTER(BatchTuning)])
+_sig("tx_batch_destroy", "argtypes", [_vp])
+_sig("tx_batch_destroy", "restype", None)
+_sig("tx_mip_count", "restype", ctypes.c_uint32)
+_sig("tx_mip_count", "argtypes", [ctypes.c_uint32, ctypes.c_uint32])
+_sig("tx_mip_batch_device", "argtypes", [ctypes.POINTER(MipJob), _sz, _vp])
 
 
 def batch_item(fmt, src_ptr, src_pitch, width, height, params, dst_ptr, channels=4):
@@ -352,17 +382,17 @@ class ServerStats(ctypes.Structure):
                 ("arena_bytes", _sz), ("arena_high_water", _sz)]
 
 
-_lib.tx_chain_compressed_size.restype = _sz
-_lib.tx_chain_compressed_size.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int]
-_lib.tx_server_default_config.argtypes = [ctypes.POINTER(ServerConfig)]
-_lib.tx_server_default_config.restype = None
-_lib.tx_server_create.argtypes = [ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)]
-_lib.tx_server_submit.argtypes = [_vp, ctypes.POINTER(ServerRequest), ctypes.POINTER(ctypes.c_uint64)]
-_lib.tx_server_wait.argtypes = [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ServerResult)]
-_lib.tx_server_get_stats.argtypes = [_vp, ctypes.POINTER(ServerStats)]
-_lib.tx_server_cancel.argtypes = [_vp, ctypes.c_uint64]
-_lib.tx_server_destroy.argtypes = [_vp]
-_lib.tx_server_destroy.restype = None
+_sig("tx_chain_compressed_size", "restype", _sz)
+_sig("tx_chain_compressed_size", "argtypes", [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_int])
+_sig("tx_server_default_config", "argtypes", [ctypes.POINTER(ServerConfig)])
+_sig("tx_server_default_config", "restype", None)
+_sig("tx_server_create", "argtypes", [ctypes.POINTER(ServerConfig), ctypes.POINTER(_vp)])
+_sig("tx_server_submit", "argtypes", [_vp, ctypes.POINTER(ServerRequest), ctypes.POINTER(ctypes.c_uint64)])
+_sig("tx_server_wait", "argtypes", [_vp, ctypes.c_uint64, ctypes.c_int, ctypes.POINTER(ServerResult)])
+_sig("tx_server_get_stats", "argtypes", [_vp, ctypes.POINTER(ServerStats)])
+_sig("tx_server_cancel", "argtypes", [_vp, ctypes.c_uint64])
+_sig("tx_server_destroy", "argtypes", [_vp])
+_sig("tx_server_destroy", "restype", None)
 
 
 def chain_compressed_size(fmt, width, height, mips=True):
@@ -442,10 +472,10 @@ class Server:
 # DDS container (tx_dds_*)
 
 DDS_HEADER_BYTES = 148
-_lib.tx_dds_write_header.argtypes = [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _sz,
-                                     ctypes.POINTER(_sz)]
-_lib.tx_dds_parse.argtypes = [_vp, _sz, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint32),
-                              ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(_sz)]
+_sig("tx_dds_write_header", "argtypes", [ctypes.c_int, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint32, _vp, _sz,
+                                         ctypes.POINTER(_sz)])
+_sig("tx_dds_parse", "argtypes", [_vp, _sz, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_uint32),
+                                  ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(_sz)])
 
 
 def dds_header(fmt, width, height, mip_levels=0):

@@ -44,6 +44,22 @@ def _deps():
     return headers
 
 
+def source_digest():
+    """16 hex digits of SHA-256 over the kernel sources (csrc/, the public
+    header) and the nvcc flags: names the build that a profiler count was
+    taken from."""
+    import hashlib
+    h = hashlib.sha256()
+    files = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h")))
+    files.append(os.path.join(ROOT, "include", "texpresso_gb300.h"))
+    for path in files:
+        h.update(os.path.basename(path).encode() + b"\0")
+        with open(path, "rb") as f:
+            h.update(f.read())
+    h.update(" ".join(f for f in NVCC_FLAGS if not f.startswith("/")).encode())
+    return h.hexdigest()[:16]
+
+
 def _needs(target, deps):
     if not os.path.exists(target):
         return True

@@ -371,7 +371,8 @@ int tx_batch_create(const tx_batch_item *items, size_t nitems, const tx_batch_tu
             it.src_pitch < (size_t)it.width * it.channels || (it.height && !it.src) || !it.dst)
             return TX_ERR_INVALID_ARGUMENT;
         if ((reinterpret_cast<uintptr_t>(it.dst) % bs) != 0) return TX_ERR_MISALIGNED;
-        if (tx_num_blocks(it.width) * tx_num_blocks(it.height) > 0xFFFFFFF0u) return TX_ERR_INVALID_ARGUMENT;
+        if (tx_num_blocks(it.width) * tx_num_blocks(it.height) > tx::kMaxBatchLevelBlocks)
+            return TX_ERR_INVALID_ARGUMENT;
     }
     int rc = tx_internal_ensure_device();
     if (rc != TX_OK) return rc;
@@ -590,8 +591,11 @@ __global__ void __launch_bounds__(kNoallocMaxItems) k_noalloc_setup(const __grid
     if (t < p.nitems) {
         const BatchItem &it = p.items[t];
         items[t] = it;
-        if (it.kind == KIND_ALPHA || it.kind == KIND_RANGE) nl = (it.nblocks + p.lane_span - 1) / p.lane_span;
-        else nt = (it.nblocks + p.team_span - 1) / p.team_span;
+        // 64-bit: nblocks < 2^31, but nblocks + span - 1 need not fit 32 bits
+        if (it.kind == KIND_ALPHA || it.kind == KIND_RANGE)
+            nl = (uint32_t)(((uint64_t)it.nblocks + p.lane_span - 1) / p.lane_span);
+        else
+            nt = (uint32_t)(((uint64_t)it.nblocks + p.team_span - 1) / p.team_span);
     }
     sl[t] = nl;
     stm[t] = nt;
@@ -665,7 +669,7 @@ extern "C" int tx_batch_launch_noalloc(const tx_batch_item *items, size_t nitems
                 return TX_ERR_INVALID_ARGUMENT;
             if ((reinterpret_cast<uintptr_t>(it.dst) % bs) != 0) return TX_ERR_MISALIGNED;
             const size_t nb = tx_num_blocks(it.width) * tx_num_blocks(it.height);
-            if (nb > 0xFFFFFFF0u) return TX_ERR_INVALID_ARGUMENT;
+            if (nb > tx::kMaxBatchLevelBlocks) return TX_ERR_INVALID_ARGUMENT;
             const bool lane = it.format == TX_FORMAT_BC4 || it.format == TX_FORMAT_BC5 || alg == TX_RANGE_FIT;
             const int kind = lane ? (alg == TX_RANGE_FIT && it.format <= TX_FORMAT_BC3 ? tx::KIND_RANGE : tx::KIND_ALPHA)
                                   : (alg == TX_ITERATIVE_CLUSTER_FIT ? tx::KIND_CLUSTER_ITER : tx::KIND_CLUSTER);
@@ -700,9 +704,9 @@ extern "C" int tx_batch_launch_noalloc(const tx_batch_item *items, size_t nitems
         for (uint32_t i = 0; i < n; ++i) {
             const tx::BatchItem &d = setup.items[i];
             if (d.kind == tx::KIND_ALPHA || d.kind == tx::KIND_RANGE) {
-                *nl += (d.nblocks + lane_span - 1) / lane_span;
+                *nl += ((uint64_t)d.nblocks + lane_span - 1) / lane_span;
             } else {
-                const uint32_t u = (d.nblocks + team_span - 1) / team_span;
+                const uint32_t u = (uint32_t)(((uint64_t)d.nblocks + team_span - 1) / team_span);
                 *nt += u;
                 team_counts[tx::team_class(d.format, d.kind)] += u;
             }

@@ -8,6 +8,11 @@ namespace tx {
 
 enum UnitKind : int32_t { KIND_ALPHA = 0, KIND_RANGE = 1, KIND_CLUSTER = 2, KIND_CLUSTER_ITER = 3 };
 
+// Most blocks one batched level may have: block numbers, a unit's first block
+// plus its span, and nblocks + span - 1 then stay below 2^32 for every span
+// the plans use.
+constexpr uint32_t kMaxBatchLevelBlocks = 0x7FFFFFFFu;
+
 struct BatchItem {
     SrcDesc src;
     DevParams prm;

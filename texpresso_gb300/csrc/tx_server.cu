@@ -535,6 +535,8 @@ int tx_server_submit(tx_server *s, const tx_server_request *req, uint64_t *id) {
     if (req->params.algorithm < TX_RANGE_FIT || req->params.algorithm > TX_ITERATIVE_CLUSTER_FIT)
         return TX_ERR_INVALID_ARGUMENT;
     if (req->width == 0 || req->height == 0 || !req->rgba) return TX_ERR_INVALID_ARGUMENT;
+    if (tx_num_blocks(req->width) * tx_num_blocks(req->height) > tx::kMaxBatchLevelBlocks)
+        return TX_ERR_INVALID_ARGUMENT;
     if (req->output_len < tx_chain_compressed_size(req->format, req->width, req->height, req->mips))
         return TX_ERR_OUTPUT_TOO_SMALL;
     if (!req->output) return TX_ERR_INVALID_ARGUMENT;
