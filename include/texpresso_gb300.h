@@ -228,7 +228,10 @@ TX_API int tx_mip_batch_device(const tx_mip_job *jobs, size_t njobs, void *strea
 
 /* ---------------------------------------------------------------------------
  * Serving form (no counterpart in the reference): a request loop that admits
- * compression jobs while a device-memory budget allows, batches every ready
+ * compression jobs first-in first-out while the bytes they hold stay within a
+ * budget and the device's free memory (cudaMemGetInfo, less 1 GiB of
+ * headroom) covers them, takes their memory from a stream-ordered pool of its
+ * own (trimmed when the server idles), batches every ready
  * job into each compression step (continuous batching: jobs that arrive while
  * others run join the next step; each job gets a round-robin share of every
  * step) and overlaps host<->device copies with compression.  A job's output
@@ -239,7 +242,7 @@ TX_API int tx_mip_batch_device(const tx_mip_job *jobs, size_t njobs, void *strea
 TX_API size_t tx_chain_compressed_size(int format, uint32_t width, uint32_t height, int mips);
 
 typedef struct tx_server_config {
-    size_t memory_budget;     /* device bytes for admitted jobs (one arena); default 40 GiB */
+    size_t memory_budget;     /* most device bytes admitted jobs may hold; default 40 GiB */
     uint32_t step_blocks;     /* blocks per compression step; default 1 Mi */
     uint32_t min_share;       /* blocks a ready job gets per step at least; default 16 Ki */
     tx_batch_tuning tuning;   /* launch shape of the step kernels (zero fields: defaults) */
@@ -265,7 +268,10 @@ typedef struct tx_server_result {
 
 typedef struct tx_server_stats {
     uint64_t submitted, completed, steps;
-    size_t arena_bytes, arena_high_water;
+    size_t memory_budget;     /* the configured budget */
+    size_t held_high_water;   /* most device bytes admitted jobs held at once */
+    double busy_us;           /* device time of the compression steps so far (CUDA events) */
+    uint64_t hbm_deferrals;   /* jobs whose admission waited for free device memory */
 } tx_server_stats;
 
 typedef struct tx_server tx_server;

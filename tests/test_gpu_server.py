@@ -88,7 +88,8 @@ def test_admission_by_memory_budget(tx, cuda, oracle):
         queued += res["queue_us"] > 0
         assert np.array_equal(out, _expected(oracle, j))
     st = srv.stats()
-    assert st["arena_high_water"] <= budget
+    assert 0 < st["held_high_water"] <= budget
+    assert st["memory_budget"] == budget and st["busy_us"] > 0
     # a job that can never fit is refused at once
     big = np.zeros((1024, 1024, 4), np.uint8)
     with pytest.raises(tx.TexpressoError) as e:
@@ -137,4 +138,36 @@ def test_wait_timeout_and_cancel(tx, cuda):
     assert srv.wait(rid, timeout_ms=60000)["status"] == 0
     for i, _ in waiting[:-1]:
         assert srv.wait(i, timeout_ms=60000)["status"] == 0
+    srv.close()
+
+
+def test_admission_waits_for_free_device_memory(tx, cuda, oracle):
+    """Admission follows the device's free memory, not only the budget: with
+    the device filled to within the headroom (1 GiB) plus a few MiB, a job of
+    about 25 MiB that the budget allows waits (the wait times out, the job is
+    kept, the deferral is counted) and runs as soon as the memory is freed."""
+    torch = cuda
+    srv = tx.Server(memory_budget=8 << 30, step_blocks=1 << 16)
+    torch.cuda.synchronize()
+    free, _ = torch.cuda.mem_get_info()
+    hold = free - (1 << 30) - (8 << 20)
+    if hold <= 0:
+        srv.close()
+        pytest.skip("device has less than the headroom free")
+    filler = torch.empty(hold, dtype=torch.uint8, device="cuda")
+    free_now, _ = torch.cuda.mem_get_info()
+    if free_now > (1 << 30) + (20 << 20):
+        del filler
+        srv.close()
+        pytest.skip("could not fill the device to within the headroom")
+    j = dict(img=workloads.ramp_texture(2048, 2048, seed=21), w=2048, h=2048, fmt=0, alg=0, aw=False, mips=True)
+    rid, out = _submit(tx, srv, j)
+    with pytest.raises(tx.TexpressoError) as e:
+        srv.wait(rid, timeout_ms=300)
+    assert e.value.status == -7
+    assert srv.stats()["hbm_deferrals"] == 1
+    del filler
+    torch.cuda.empty_cache()
+    assert srv.wait(rid, timeout_ms=60000)["status"] == 0
+    assert np.array_equal(out, _expected(oracle, j))
     srv.close()

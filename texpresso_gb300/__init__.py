@@ -379,7 +379,8 @@ class ServerResult(ctypes.Structure):
 
 class ServerStats(ctypes.Structure):
     _fields_ = [("submitted", ctypes.c_uint64), ("completed", ctypes.c_uint64), ("steps", ctypes.c_uint64),
-                ("arena_bytes", _sz), ("arena_high_water", _sz)]
+                ("memory_budget", _sz), ("held_high_water", _sz), ("busy_us", ctypes.c_double),
+                ("hbm_deferrals", ctypes.c_uint64)]
 
 
 _sig("tx_chain_compressed_size", "restype", _sz)
@@ -453,7 +454,7 @@ class Server:
     def stats(self):
         s = ServerStats()
         _check(_lib.tx_server_get_stats(self._h, ctypes.byref(s)), "tx_server_get_stats")
-        return {f: int(getattr(s, f)) for f, _ in s._fields_}
+        return {f: (float if t is ctypes.c_double else int)(getattr(s, f)) for f, t in s._fields_}
 
     def close(self):
         if getattr(self, "_h", None):

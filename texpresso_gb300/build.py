@@ -44,15 +44,16 @@ def _deps():
     return headers
 
 
+# Device code of the single-texture kernels (k_cluster, k_range, k_alpha).
+KERNEL_SOURCES = ("tx_alpha.cu", "tx_alpha.cuh", "tx_colour.cu", "tx_colour.cuh", "tx_device.cuh")
+
+
 def source_digest():
-    """16 hex digits of SHA-256 over the kernel sources (csrc/, the public
-    header) and the nvcc flags: names the build that a profiler count was
-    taken from."""
+    """16 hex digits of SHA-256 over the single-texture kernels' device code
+    and the nvcc flags: names the build that a profiler count was taken from."""
     import hashlib
     h = hashlib.sha256()
-    files = sorted(os.path.join(CSRC, f) for f in os.listdir(CSRC) if f.endswith((".cu", ".cuh", ".h")))
-    files.append(os.path.join(ROOT, "include", "texpresso_gb300.h"))
-    for path in files:
+    for path in (os.path.join(CSRC, f) for f in KERNEL_SOURCES):
         h.update(os.path.basename(path).encode() + b"\0")
         with open(path, "rb") as f:
             h.update(f.read())

@@ -1,21 +1,27 @@
-// tx_server.cu -- serving form: a request loop with admission by device memory
-// and continuous batching.
+// tx_server.cu -- serving form: a request loop with admission by free device
+// memory and continuous batching.
 //
-// A server owns one device-memory arena (the admission budget), three streams
-// (host->device copies and mip generation, compression steps, device->host
-// copies) and one worker thread.  Requests are admitted first-in first-out as
-// arena space frees up; an admitted request's pixels are copied in and its mip
-// chain built on the copy stream, overlapping the running compression steps.
-// Every step is one launch of the persistent batch kernels over a work queue
-// assembled from all ready requests: each gets a round-robin share of blocks,
-// so requests that arrive while others run join the very next step and small
-// requests finish without waiting for large ones.  Two steps are kept in
-// flight; the queue of step n+1 is written while step n runs.  When a request's
-// last blocks have been compressed its levels are copied back on the third
-// stream and its arena space is released.
+// A server owns a stream-ordered memory pool, three streams (host->device
+// copies and mip generation, compression steps, device->host copies) and one
+// worker thread.  Requests are admitted first-in first-out while two limits
+// allow: the bytes held by admitted requests stay within the budget, and the
+// device's free memory right now (cudaMemGetInfo, plus what the pool holds
+// but no request uses) covers the request with a fixed headroom left over for
+// everything else on the device.  An admitted request gets its device memory
+// from the pool on the copy stream; its pixels are copied in and its mip chain
+// built there, overlapping the running compression steps.  Every step is one
+// launch of the persistent batch kernels over a work queue assembled from all
+// ready requests: each gets a round-robin share of blocks, so requests that
+// arrive while others run join the very next step and small requests finish
+// without waiting for large ones.  Two steps are kept in flight; the queue of
+// step n+1 is written while step n runs.  When a request's last blocks have
+// been compressed its levels are copied back on the third stream and its
+// memory goes back to the pool behind those copies.
 //
 // Each block is encoded by the same per-block code as every other entry point,
-// so a request's bytes do not depend on what else is in flight.
+// so a request's bytes do not depend on what else is in flight.  The loop is
+// scheduled from the host: a step is a kernel launch, so no kernel waits on
+// another or on the host.
 #include "texpresso_gb300.h"
 #include "tx_batch_internal.h"
 #include "tx_internal.h"
@@ -45,51 +51,9 @@ double now_us() {
 constexpr size_t kAlign = 256;
 size_t align_up(size_t v) { return (v + kAlign - 1) & ~(kAlign - 1); }
 
-// First-fit allocator over [0, size) with coalescing frees.
-class Arena {
-  public:
-    void reset(size_t size) {
-        free_.clear();
-        if (size) free_[0] = size;
-        used_ = 0;
-        high_ = 0;
-    }
-    bool alloc(size_t n, size_t *off) {
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second >= n) {
-                *off = it->first;
-                const size_t rest = it->second - n, start = it->first + n;
-                free_.erase(it);
-                if (rest) free_[start] = rest;
-                used_ += n;
-                high_ = std::max(high_, used_);
-                return true;
-            }
-        }
-        return false;
-    }
-    void release(size_t off, size_t n) {
-        used_ -= n;
-        auto it = free_.emplace(off, n).first;
-        auto next = std::next(it);
-        if (next != free_.end() && it->first + it->second == next->first) {
-            it->second += next->second;
-            free_.erase(next);
-        }
-        if (it != free_.begin()) {
-            auto prev = std::prev(it);
-            if (prev->first + prev->second == it->first) {
-                prev->second += it->second;
-                free_.erase(it);
-            }
-        }
-    }
-    size_t high() const { return high_; }
-
-  private:
-    std::map<size_t, size_t> free_;
-    size_t used_ = 0, high_ = 0;
-};
+// Device memory left free for everything else on the device (other
+// libraries' caches, other processes) when admitting a request.
+constexpr size_t kHbmHeadroom = (size_t)1 << 30;
 
 struct Level {
     uint32_t w, h, nblocks;
@@ -100,7 +64,8 @@ struct Request {
     uint64_t id = 0;
     tx_server_request r{};
     std::vector<Level> levels;
-    size_t footprint = 0, arena_off = 0;
+    size_t footprint = 0;
+    uint8_t *dev = nullptr;  // the request's device memory (from the server's pool)
     enum State { QUEUED, LOADING, ACTIVE, DRAINING, DONE } state = QUEUED;
     std::vector<uint32_t> next_block;
     size_t unassigned = 0;
@@ -108,6 +73,7 @@ struct Request {
     double t_submit = 0, t_admit = 0, t_done = 0;
     int status = TX_OK;
     uint32_t steps = 0;
+    bool hbm_deferred = false;          // worker only: counted once in hbm_waits
     std::atomic<bool> finished{false};  // set under tx_server::mu; read by waiters
     bool cancel = false;                // guarded by tx_server::mu
     bool admitted = false;              // guarded by tx_server::mu
@@ -119,7 +85,7 @@ struct Step {
     uint32_t *d_counters = nullptr;
     tx::BatchItem *h_items = nullptr;  // pinned staging
     uint2 *h_units = nullptr;          // pinned staging
-    cudaEvent_t done = nullptr;
+    cudaEvent_t start = nullptr, done = nullptr;  // timing: the step's time on the compression stream
     std::vector<Request *> finishing;
     bool busy = false;
 };
@@ -129,8 +95,10 @@ struct Step {
 struct tx_server {
     tx_server_config cfg{};
     int device = 0, sm_count = 0;
-    uint8_t *arena_base = nullptr;
-    Arena arena;
+    cudaMemPool_t pool = nullptr;
+    size_t held = 0, held_high = 0;  // bytes held by admitted requests (worker only; stats under mu)
+    double busy_us = 0;              // compression-step time on the device (worker only; stats under mu)
+    uint64_t hbm_waits = 0;          // admissions deferred for lack of free device memory
     cudaStream_t s_load = nullptr, s_comp = nullptr, s_store = nullptr;
     Step steps[2];
     uint32_t max_items = 0, max_units = 0;
@@ -194,8 +162,26 @@ void finish_cancelled(tx_server *s, Request *q) {  // caller holds s->mu
     s->cv_done.notify_all();
 }
 
-// Admit the head of the waiting line while arena space lasts (FIFO).
+// Device memory an admission may take now: the device's free memory plus
+// what the pool holds that no request uses, less the headroom.
+cudaError_t hbm_available(tx_server *s, size_t *avail) {
+    size_t fr = 0, total = 0;
+    cudaError_t e = cudaMemGetInfo(&fr, &total);
+    if (e != cudaSuccess) return e;
+    uint64_t reserved = 0, used = 0;  // the attributes are 64-bit values
+    if ((e = cudaMemPoolGetAttribute(s->pool, cudaMemPoolAttrReservedMemCurrent, &reserved)) != cudaSuccess) return e;
+    if ((e = cudaMemPoolGetAttribute(s->pool, cudaMemPoolAttrUsedMemCurrent, &used)) != cudaSuccess) return e;
+    const size_t a = fr + (size_t)(reserved > used ? reserved - used : 0);
+    *avail = a > kHbmHeadroom ? a - kHbmHeadroom : 0;
+    return cudaSuccess;
+}
+
+// Admit the head of the waiting line while the budget and the device's free
+// memory allow (FIFO: a request that does not fit holds back the ones behind
+// it, so a large request is never starved by small ones).
 int admit(tx_server *s) {
+    bool queried = false;
+    size_t avail = 0;
     while (!s->waiting.empty()) {
         Request *q = s->waiting.front();
         {
@@ -206,27 +192,49 @@ int admit(tx_server *s) {
                 continue;
             }
         }
-        size_t off = 0;
-        if (!s->arena.alloc(q->footprint, &off)) break;
+        if (s->held + q->footprint > s->cfg.memory_budget) break;
+        cudaError_t e;
+        if (!queried || avail < q->footprint) {
+            if ((e = hbm_available(s, &avail)) != cudaSuccess) return fail_server(e);
+            queried = true;
+        }
+        if (avail < q->footprint) {
+            if (!q->hbm_deferred) {
+                q->hbm_deferred = true;
+                std::lock_guard<std::mutex> lk(s->mu);
+                s->hbm_waits++;
+            }
+            break;
+        }
+        void *ptr = nullptr;
+        e = cudaMallocFromPoolAsync(&ptr, q->footprint, s->pool, s->s_load);
+        if (e == cudaErrorMemoryAllocation) {  // lost a race for the memory: retry later
+            cudaGetLastError();
+            avail = 0;
+            break;
+        }
+        if (e != cudaSuccess) return fail_server(e);
+        avail -= q->footprint;
         {
             std::lock_guard<std::mutex> lk(s->mu);
             if (q->cancel) {  // cancelled between the check and the allocation
-                s->arena.release(off, q->footprint);
+                if ((e = cudaFreeAsync(ptr, s->s_load)) != cudaSuccess) return fail_server(e);
                 s->waiting.pop_front();
                 finish_cancelled(s, q);
                 continue;
             }
             q->admitted = true;
+            s->held += q->footprint;
+            s->held_high = std::max(s->held_high, s->held);
         }
         nvtxRangePushA("tx_server admit");
         s->waiting.pop_front();
-        q->arena_off = off;
+        q->dev = static_cast<uint8_t *>(ptr);
         q->t_admit = now_us();
         q->state = Request::LOADING;
-        uint8_t *base = s->arena_base + off;
+        uint8_t *base = q->dev;
         const Level &l0 = q->levels[0];
-        cudaError_t e = cudaMemcpyAsync(base + l0.src_off, q->r.rgba, (size_t)l0.w * l0.h * 4, cudaMemcpyHostToDevice,
-                                        s->s_load);
+        e = cudaMemcpyAsync(base + l0.src_off, q->r.rgba, (size_t)l0.w * l0.h * 4, cudaMemcpyHostToDevice, s->s_load);
         if (e != cudaSuccess) return fail_server(e);
         for (size_t l = 1; l < q->levels.size(); ++l) {
             const Level &a = q->levels[l - 1], &b = q->levels[l];
@@ -267,14 +275,14 @@ int schedule_step(tx_server *s) {
             if (nb >= lv.nblocks) continue;
             const uint32_t n = (uint32_t)std::min<size_t>(take, lv.nblocks - nb);
             tx_batch_item it{};
-            it.src = s->arena_base + q->arena_off + lv.src_off;
+            it.src = q->dev + lv.src_off;
             it.src_pitch = (size_t)lv.w * 4;
             it.width = lv.w;
             it.height = lv.h;
             it.format = q->r.format;
             it.channels = 4;
             it.params = q->r.params;
-            it.dst = s->arena_base + q->arena_off + lv.dst_off;
+            it.dst = q->dev + lv.dst_off;
             tx::fill_batch_item(it, &st.h_items[n_items]);
             const tx::BatchItem &d = st.h_items[n_items];
             const bool lane = d.kind == tx::KIND_ALPHA || d.kind == tx::KIND_RANGE;
@@ -307,6 +315,7 @@ int schedule_step(tx_server *s) {
         std::memcpy(st.h_units + off, class_units[c].data(), team_counts[c] * sizeof(uint2));
     cudaError_t e;
     nvtxRangePushA("tx_server step");
+    if ((e = cudaEventRecord(st.start, s->s_comp)) != cudaSuccess) return fail_server(e);
     if ((e = cudaMemcpyAsync(st.d_items, st.h_items, n_items * sizeof(tx::BatchItem), cudaMemcpyHostToDevice,
                              s->s_comp)) != cudaSuccess)
         return fail_server(e);
@@ -334,8 +343,14 @@ int retire_steps(tx_server *s) {
         cudaError_t e = cudaEventQuery(st.done);
         if (e == cudaErrorNotReady) return TX_OK;  // steps complete in order
         if (e != cudaSuccess) return fail_server(e);
+        float ms = 0.0f;
+        if ((e = cudaEventElapsedTime(&ms, st.start, st.done)) != cudaSuccess) return fail_server(e);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->busy_us += (double)ms * 1e3;
+        }
         for (Request *q : st.finishing) {
-            uint8_t *base = s->arena_base + q->arena_off;
+            uint8_t *base = q->dev;
             if ((e = cudaStreamWaitEvent(s->s_store, st.done, 0)) != cudaSuccess) return fail_server(e);
             for (const Level &lv : q->levels) {
                 if (lv.dst_bytes == 0) continue;
@@ -371,8 +386,11 @@ int progress(tx_server *s, bool *completed_any) {
         } else if (q->state == Request::DRAINING) {
             cudaError_t e = cudaEventQuery(q->done_ev);
             if (e == cudaSuccess) {
-                s->arena.release(q->arena_off, q->footprint);
+                // back to the pool behind the copies (done_ev has completed)
+                if ((e = cudaFreeAsync(q->dev, s->s_store)) != cudaSuccess) return fail_server(e);
+                q->dev = nullptr;
                 std::lock_guard<std::mutex> lk(s->mu);
+                s->held -= q->footprint;
                 q->t_done = now_us();
                 q->state = Request::DONE;
                 q->finished.store(true);
@@ -406,13 +424,20 @@ void fail_all(tx_server *s, int rc) {
 
 void worker_main(tx_server *s) {
     cudaSetDevice(s->device);
+    bool idle = false;
     for (;;) {
         {
             std::unique_lock<std::mutex> lk(s->mu);
             if (s->fatal != TX_OK) return;
             if (s->submitted.empty() && s->waiting.empty() && s->live.empty()) {
                 if (s->stopping) return;
+                if (!idle) {  // nothing admitted: give the pool's memory back to the device
+                    cudaMemPoolTrimTo(s->pool, 0);
+                    idle = true;
+                }
                 s->cv_work.wait_for(lk, std::chrono::milliseconds(5));
+            } else {
+                idle = false;
             }
             while (!s->submitted.empty()) {
                 s->waiting.push_back(s->submitted.front());
@@ -443,9 +468,10 @@ void destroy_resources(tx_server *s) {
         cudaFree(st.d_counters);
         cudaFreeHost(st.h_items);
         cudaFreeHost(st.h_units);
+        if (st.start) cudaEventDestroy(st.start);
         if (st.done) cudaEventDestroy(st.done);
     }
-    cudaFree(s->arena_base);
+    if (s->pool) cudaMemPoolDestroy(s->pool);
     if (s->s_load) cudaStreamDestroy(s->s_load);
     if (s->s_comp) cudaStreamDestroy(s->s_comp);
     if (s->s_store) cudaStreamDestroy(s->s_store);
@@ -506,7 +532,18 @@ int tx_server_create(const tx_server_config *config, tx_server **out) {
     cudaDeviceGetAttribute(&s->sm_count, cudaDevAttrMultiProcessorCount, s->device);
     s->max_items = 65536;
     s->max_units = cfg.step_blocks + s->max_items * 2;
-    cudaError_t e = cudaMalloc(&s->arena_base, cfg.memory_budget);
+    // requests' device memory: a pool of the server's own, which keeps up to
+    // the budget mapped between requests and is trimmed when the server idles
+    cudaMemPoolProps props;
+    std::memset(&props, 0, sizeof(props));
+    props.allocType = cudaMemAllocationTypePinned;
+    props.location.type = cudaMemLocationTypeDevice;
+    props.location.id = s->device;
+    cudaError_t e = cudaMemPoolCreate(&s->pool, &props);
+    if (e == cudaSuccess) {
+        uint64_t keep = cfg.memory_budget;
+        e = cudaMemPoolSetAttribute(s->pool, cudaMemPoolAttrReleaseThreshold, &keep);
+    }
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s_load, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s_comp, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&s->s_store, cudaStreamNonBlocking);
@@ -516,14 +553,14 @@ int tx_server_create(const tx_server_config *config, tx_server **out) {
         if (e == cudaSuccess) e = cudaMalloc(&st.d_counters, tx::kBatchCounters * sizeof(uint32_t));
         if (e == cudaSuccess) e = cudaMallocHost(&st.h_items, s->max_items * sizeof(tx::BatchItem));
         if (e == cudaSuccess) e = cudaMallocHost(&st.h_units, s->max_units * sizeof(uint2));
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&st.done, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventCreate(&st.start);
+        if (e == cudaSuccess) e = cudaEventCreate(&st.done);
     }
     if (e != cudaSuccess) {
         destroy_resources(s);
         delete s;
         return fail_server(e);
     }
-    s->arena.reset(cfg.memory_budget);
     s->worker = std::thread(worker_main, s);
     *out = s;
     return TX_OK;
@@ -631,8 +668,10 @@ int tx_server_get_stats(tx_server *s, tx_server_stats *out) {
     out->submitted = s->n_submitted;
     out->completed = s->n_completed;
     out->steps = s->step_count;
-    out->arena_bytes = s->cfg.memory_budget;
-    out->arena_high_water = s->arena.high();
+    out->memory_budget = s->cfg.memory_budget;
+    out->held_high_water = s->held_high;
+    out->busy_us = s->busy_us;
+    out->hbm_deferrals = s->hbm_waits;
     return TX_OK;
 }
 
@@ -646,6 +685,9 @@ void tx_server_destroy(tx_server *s) {
     if (s->worker.joinable()) s->worker.join();
     cudaStreamSynchronize(s->s_load);
     cudaStreamSynchronize(s->s_comp);
+    cudaStreamSynchronize(s->s_store);
+    for (Request *q : s->live)  // only after a fatal error: requests that still hold memory
+        if (q->dev) cudaFreeAsync(q->dev, s->s_store);
     cudaStreamSynchronize(s->s_store);
     for (auto &kv : s->requests) {
         cudaEventDestroy(kv.second->ready_ev);
