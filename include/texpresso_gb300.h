@@ -157,6 +157,8 @@ typedef struct tx_batch_tuning {
     int32_t team_blocks_per_unit;  /* ClusterFit blocks a team takes per queue pop */
     int32_t lane_ctas_per_sm;      /* RangeFit/BC4/BC5 kernel: persistent grid = SMs x this */
     int32_t lane_blocks_per_lane;  /* blocks per lane per queue pop (units of 32 x this) */
+    int32_t team_blocks_in_flight; /* staging depth of the ClusterFit kernel: blocks whose pixels a team
+                                    * holds or has requested, 1 (none ahead) to 3 (two ahead) */
 } tx_batch_tuning;
 
 typedef struct tx_batch tx_batch;  /* opaque plan; not thread-safe */

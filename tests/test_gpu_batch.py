@@ -59,9 +59,13 @@ def test_batch_equals_per_call_and_oracle(tx, cuda, tset, oracle):
 
 @pytest.mark.parametrize("tuning", [
     dict(team_lanes=16, team_threads_per_cta=128, team_ctas_per_sm=2, team_blocks_per_unit=3,
-         lane_ctas_per_sm=2, lane_blocks_per_lane=1),
+         lane_ctas_per_sm=2, lane_blocks_per_lane=1, team_blocks_in_flight=1),
     dict(team_lanes=32, team_threads_per_cta=64, team_ctas_per_sm=1, team_blocks_per_unit=8,
-         lane_ctas_per_sm=6, lane_blocks_per_lane=8),
+         lane_ctas_per_sm=6, lane_blocks_per_lane=8, team_blocks_in_flight=3),
+    dict(team_lanes=32, team_threads_per_cta=256, team_ctas_per_sm=4, team_blocks_per_unit=5,
+         lane_ctas_per_sm=3, lane_blocks_per_lane=2, team_blocks_in_flight=2),
+    dict(team_lanes=16, team_threads_per_cta=256, team_ctas_per_sm=3, team_blocks_per_unit=1,
+         lane_ctas_per_sm=4, lane_blocks_per_lane=3, team_blocks_in_flight=3),
 ])
 def test_launch_shapes_do_not_change_bytes(tx, cuda, tset, tuning):
     from texpresso_gb300.texture_set import same

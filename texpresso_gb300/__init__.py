@@ -259,7 +259,8 @@ class BatchTuning(ctypes.Structure):
     """tx_batch_tuning: launch shape of the persistent batch kernels."""
     _fields_ = [("team_lanes", ctypes.c_int32), ("team_threads_per_cta", ctypes.c_int32),
                 ("team_ctas_per_sm", ctypes.c_int32), ("team_blocks_per_unit", ctypes.c_int32),
-                ("lane_ctas_per_sm", ctypes.c_int32), ("lane_blocks_per_lane", ctypes.c_int32)]
+                ("lane_ctas_per_sm", ctypes.c_int32), ("lane_blocks_per_lane", ctypes.c_int32),
+                ("team_blocks_in_flight", ctypes.c_int32)]
 
     def as_dict(self):
         return {f: int(getattr(self, f)) for f, _ in self._fields_}

@@ -37,65 +37,12 @@
 
 namespace tx {
 
-cudaError_t upload_batch_tables(const uint32_t lut[4][256][2]) { return upload_tables_this_tu(lut); }
-
-// One team class: every unit of q is (FMT, NITER).
-template <int TEAM, int FMT, int NITER>
-__global__ void __launch_bounds__(256, 4) k_batch_teams(BatchQueue q) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    __shared__ float s_unorm[256];
-    __shared__ float s_sqrt[17];
-    init_unorm_tables(s_unorm, s_sqrt);
-    TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw);
-    const TeamTables tt{g_cand, g_cand + kCand4 + 1, s_unorm, s_sqrt};
-    const Team<TEAM> tm;
-    TeamSmem &sm = teams[threadIdx.x / TEAM];
-    if (NITER == 1) {
-        for (;;) {
-            uint32_t u = 0;
-            if (tm.lane == 0) u = atomicAdd(q.counter, 1u);
-            u = tm.shfl(u, 0);
-            if (u >= q.nunits) break;
-            const uint2 unit = q.units[u];
-            const BatchItem &it = q.items[unit.x];
-            const SrcDesc src = it.src;
-            const DevParams prm = it.prm;
-            uint8_t *dst = it.dst;
-            const uint32_t end = min(unit.y + q.per_unit, it.nblocks);
-            for (uint32_t b = unit.y; b < end; ++b) cluster_block<FMT, TEAM, NITER>(tm, sm, tt, src, b, prm, dst);
-        }
-        return;
-    }
-    // IterativeClusterFit: a block takes long enough that the queue pop and
-    // the pixel loads of the next block are issued before the current block
-    // is encoded, so their latency hides behind it.
-    auto pop = [&](uint32_t &item, uint32_t &b, uint32_t &end) {
-        uint32_t u = 0;
-        if (tm.lane == 0) u = atomicAdd(q.counter, 1u);
-        u = tm.shfl(u, 0);
-        if (u >= q.nunits) return false;
-        const uint2 unit = q.units[u];
-        item = unit.x;
-        b = unit.y;
-        end = min(unit.y + q.per_unit, q.items[unit.x].nblocks);
-        return true;
-    };
-    uint32_t ci, cb, ce;
-    if (!pop(ci, cb, ce)) return;
-    TeamPixel tp = load_team_pixel(q.items[ci].src, cb, tm.lane);
-    for (;;) {
-        uint32_t ni = ci, nb = cb + 1, ne = ce;
-        const bool more = nb < ne || pop(ni, nb, ne);
-        TeamPixel tn{0u, false};
-        if (more) tn = load_team_pixel(q.items[ni].src, nb, tm.lane);
-        const BatchItem &it = q.items[ci];
-        cluster_block_px<FMT, TEAM, NITER>(tm, sm, tt, tp, cb, it.prm, it.dst);
-        if (!more) break;
-        ci = ni;
-        cb = nb;
-        ce = ne;
-        tp = tn;
-    }
+cudaError_t upload_batch_tables(const uint32_t lut[4][256][2]) {
+    cudaError_t e = upload_tables_this_tu(lut);  // this unit's lane kernel
+    if (e == cudaSuccess) e = upload_stage_tables<1>(lut);
+    if (e == cudaSuccess) e = upload_stage_tables<2>(lut);
+    if (e == cudaSuccess) e = upload_stage_tables<3>(lut);
+    return e;
 }
 
 __global__ void __launch_bounds__(128) k_batch_lanes(BatchQueue q) {
@@ -203,6 +150,7 @@ void default_tuning(tx_batch_tuning *t) {
     t->team_blocks_per_unit = 1;
     t->lane_ctas_per_sm = 3;
     t->lane_blocks_per_lane = 2;
+    t->team_blocks_in_flight = 2;
 }
 
 void fill_tuning(const tx_batch_tuning *in, tx_batch_tuning *out) {
@@ -216,6 +164,8 @@ void fill_tuning(const tx_batch_tuning *in, tx_batch_tuning *out) {
     if (in->team_blocks_per_unit >= 1 && in->team_blocks_per_unit <= 64) out->team_blocks_per_unit = in->team_blocks_per_unit;
     if (in->lane_ctas_per_sm >= 1 && in->lane_ctas_per_sm <= 16) out->lane_ctas_per_sm = in->lane_ctas_per_sm;
     if (in->lane_blocks_per_lane >= 1 && in->lane_blocks_per_lane <= 64) out->lane_blocks_per_lane = in->lane_blocks_per_lane;
+    if (in->team_blocks_in_flight >= 1 && in->team_blocks_in_flight <= 3)
+        out->team_blocks_in_flight = in->team_blocks_in_flight;
 }
 
 int fail_batch(cudaError_t e) {
@@ -504,6 +454,7 @@ int tx_batch_autotune(tx_batch *b, void *stream, int repeats, tx_batch_tuning *c
             {&tx_batch_tuning::team_threads_per_cta, {64, 128, 256}, 3, true},
             {&tx_batch_tuning::team_ctas_per_sm, {1, 2, 3, 4, 6, 8}, 6, true},
             {&tx_batch_tuning::team_blocks_per_unit, {1, 2, 4, 8}, 4, true},
+            {&tx_batch_tuning::team_blocks_in_flight, {1, 2, 3}, 3, true},
             {&tx_batch_tuning::lane_ctas_per_sm, {2, 3, 4, 6}, 4, false},
             {&tx_batch_tuning::lane_blocks_per_lane, {1, 2, 4, 8}, 4, false},
         };
@@ -783,52 +734,9 @@ void fill_batch_item(const tx_batch_item &it, BatchItem *d) {
     else d->kind = alg == TX_ITERATIVE_CLUSTER_FIT ? KIND_CLUSTER_ITER : KIND_CLUSTER;
 }
 
-// The team kernels need more than 48 KB of dynamic shared memory: raise the
-// limit once per device and kernel.
-template <int TEAM, int FMT, int NITER>
-static cudaError_t class_attr() {
-    static bool attr_set[64] = {};
-    int dev = 0;
-    cudaGetDevice(&dev);
-    if (dev < 64 && !attr_set[dev]) {
-        const cudaError_t e = cudaFuncSetAttribute(k_batch_teams<TEAM, FMT, NITER>,
-                                                   cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                                   (int)cluster_smem_bytes(TEAM, 256));
-        if (e != cudaSuccess) return e;
-        attr_set[dev] = true;
-    }
-    return cudaSuccess;
-}
-
 cudaError_t prepare_team_kernels() {
-    cudaError_t e;
-    if ((e = class_attr<32, BC1, 8>()) != cudaSuccess || (e = class_attr<32, BC2, 8>()) != cudaSuccess ||
-        (e = class_attr<32, BC3, 8>()) != cudaSuccess || (e = class_attr<32, BC1, 1>()) != cudaSuccess ||
-        (e = class_attr<32, BC2, 1>()) != cudaSuccess || (e = class_attr<32, BC3, 1>()) != cudaSuccess)
-        return e;
-    return cudaSuccess;
-}
-
-template <int TEAM, int FMT, int NITER>
-static cudaError_t launch_one_class(const BatchQueue &q, uint32_t grid, int threads, cudaStream_t st) {
-    const cudaError_t e = class_attr<TEAM, FMT, NITER>();
-    if (e != cudaSuccess) return e;
-    k_batch_teams<TEAM, FMT, NITER><<<grid, threads, cluster_smem_bytes(TEAM, threads), st>>>(q);
-    note_launch();
-    return cudaGetLastError();
-}
-
-template <int TEAM>
-static cudaError_t launch_class(int c, const BatchQueue &q, uint32_t grid, int threads, cudaStream_t st) {
-    switch (c) {
-    case 0: return launch_one_class<TEAM, BC1, 8>(q, grid, threads, st);
-    case 1: return launch_one_class<TEAM, BC2, 8>(q, grid, threads, st);
-    case 2: return launch_one_class<TEAM, BC3, 8>(q, grid, threads, st);
-    case 3: return launch_one_class<TEAM, BC1, 1>(q, grid, threads, st);
-    case 4: return launch_one_class<TEAM, BC2, 1>(q, grid, threads, st);
-    case 5: return launch_one_class<TEAM, BC3, 1>(q, grid, threads, st);
-    default: return cudaErrorInvalidValue;
-    }
+    // the default staging depth, the one the allocation-free launch uses
+    return prepare_team_class_kernels<2>();
 }
 
 cudaError_t launch_team_classes(const BatchItem *d_items, const uint2 *d_team,
@@ -845,8 +753,9 @@ cudaError_t launch_team_classes(const BatchItem *d_items, const uint2 *d_team,
         grid = std::max<uint32_t>(1, std::min<uint32_t>(grid, (n + per - 1) / per));
         const BatchQueue q{d_items, d_team + begin, n, counters + c, team_blocks_per_unit};
         begin += n;
-        const cudaError_t e = team == 16 ? launch_class<16>(c, q, grid, threads, st)
-                                         : launch_class<32>(c, q, grid, threads, st);
+        const cudaError_t e = t.team_blocks_in_flight == 1   ? launch_team_class<1>(team, c, q, grid, threads, st)
+                              : t.team_blocks_in_flight == 3 ? launch_team_class<3>(team, c, q, grid, threads, st)
+                                                             : launch_team_class<2>(team, c, q, grid, threads, st);
         if (e != cudaSuccess) return e;
     }
     return cudaSuccess;

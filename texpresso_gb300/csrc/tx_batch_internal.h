@@ -56,6 +56,17 @@ cudaError_t launch_team_classes(const BatchItem *d_items, const uint2 *d_team,
 // the current device (done by a plain launch on first use otherwise).
 cudaError_t prepare_team_kernels();
 
+// The team kernels with STAGE blocks in flight per team (1-3), one
+// translation unit each (tx_batch_stage<STAGE>.cu, tx_batch_teams.cuh):
+// launch the kernel of class c (see team_class) with `team` lanes per block,
+// raise their shared-memory limits, and upload that unit's constant tables.
+template <int STAGE>
+cudaError_t launch_team_class(int team, int c, const BatchQueue &q, uint32_t grid, int threads, cudaStream_t st);
+template <int STAGE>
+cudaError_t prepare_team_class_kernels();
+template <int STAGE>
+cudaError_t upload_stage_tables(const uint32_t lut[4][256][2]);
+
 // Enqueue the lane kernel and the team kernels over device-resident queues on
 // `st` (sequentially).  counters[0 .. kBatchCounters) must be zero when the
 // kernels start.

@@ -165,6 +165,40 @@ struct PointCol {
     __device__ __forceinline__ float4 &operator[](int i) const { return base[i * stride]; }
 };
 
+// The duplicate search of ColourSet::new (colourset.rs:82-102) for one block:
+// each pixel's point is the first pixel with its key, and a point's pixel
+// count is one plus the later pixels that join it.  res (4 words) receives
+// byte p = pixel p's point index | (count - 1) << 4 (the count half is kept
+// for points only).  Keys: the RGB of a valid pixel, or 0x01000000 | p for a
+// pixel that is not (so it matches nothing).
+__device__ __forceinline__ void colour_dedup(const uint32_t (&key)[16], uint32_t (&res)[4]) {
+    uint64_t repn = 0, dupc = 0;  // nibble p: point index of pixel p / later pixels joining point p
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+        int r = i;
+#pragma unroll
+        for (int j = i - 1; j >= 0; --j) r = (key[j] == key[i]) ? j : r;
+        repn |= (uint64_t)r << (4 * i);
+        if (r != i) dupc += 1ull << (4 * r);
+    }
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        uint32_t x = 0;
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+            const int i = 4 * w + c;
+            x |= (uint32_t)(((repn >> (4 * i)) & 0xFu) | (((dupc >> (4 * i)) & 0xFu) << 4)) << (8 * c);
+        }
+        res[w] = x;
+    }
+}
+
+// Point index and (pixel count - 1) of pixel i from colour_dedup's bytes.
+__device__ __forceinline__ uint32_t dd_rep(const uint32_t (&res)[4], int i) { return (res[i >> 2] >> (8 * (i & 3))) & 0xFu; }
+__device__ __forceinline__ uint32_t dd_dup(const uint32_t (&res)[4], int i) {
+    return (res[i >> 2] >> (8 * (i & 3) + 4)) & 0xFu;
+}
+
 template <int FMT>
 __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], uint32_t inb,
                                                      const DevParams &prm, const float *s_unorm,
@@ -179,25 +213,22 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
     }
     const uint32_t valid = inb & ~tbits;
     const bool transparent = tbits != 0;
-    uint32_t newbits = 0;
-    uint64_t repn = 0;  // nibble p: pixel index of p's first occurrence
-    uint64_t dupc = 0;  // nibble p: further pixels sharing p's colour
+    uint32_t dd[4];  // byte p: pixel p's point index | (its colour's pixel count - 1) << 4
     {
         uint32_t key[16];
 #pragma unroll
         for (int i = 0; i < 16; ++i) key[i] = ((valid >> i) & 1u) ? (px[i] & 0xFFFFFFu) : (0x01000000u | (uint32_t)i);
-#pragma unroll
-        for (int i = 0; i < 16; ++i) {
-            int r = i;
-#pragma unroll
-            for (int j = i - 1; j >= 0; --j) r = (key[j] == key[i]) ? j : r;
-            repn |= (uint64_t)r << (4 * i);
-            if ((valid >> i) & 1u) {
-                if (r == i) newbits |= 1u << i;
-                else dupc += 1ull << (4 * r);
-            }
-        }
+        colour_dedup(key, dd);
     }
+    // a valid pixel that is its own point starts a new point (excluded pixels
+    // match nothing, so they are their own "point" too and are masked out)
+    uint32_t newbits = 0;
+#pragma unroll
+    for (int w = 0; w < 4; ++w) {
+        const uint32_t eq = bytes_eq(dd[w] & 0x0F0F0F0Fu, 0x03020100u + 0x04040404u * (uint32_t)w);
+        newbits |= (((eq & 0x08040201u) * 0x01010101u) >> 24) << (4 * w);
+    }
+    newbits &= valid;
     const int count = __popc(newbits);
 
     if (count == 1) {
@@ -219,7 +250,7 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
     if (!prm.alpha_weighted) {
 #pragma unroll
         for (int i = 0; i < 16; ++i) {
-            const float w = ((newbits >> i) & 1u) ? s_sqrt[1 + (int)((dupc >> (4 * i)) & 0xFu)] : 0.0f;
+            const float w = ((newbits >> i) & 1u) ? s_sqrt[1 + (int)dd_dup(dd, i)] : 0.0f;
             pt[i] = make_float4(s_unorm[u8_of(px[i], 0)], s_unorm[u8_of(px[i], 1)], s_unorm[u8_of(px[i], 2)], w);
         }
     } else {
@@ -229,7 +260,7 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
 #pragma unroll
             for (int i = j; i < 16; ++i) {
                 const float wa = (float)((px[i] >> 24) + 1u) * (1.0f / 256.0f);
-                acc = acc + ((((valid >> i) & 1u) && (int)((repn >> (4 * i)) & 0xFu) == j) ? wa : 0.0f);
+                acc = acc + ((((valid >> i) & 1u) && (int)dd_rep(dd, i) == j) ? wa : 0.0f);
             }
             const float w = ((newbits >> j) & 1u) ? sqrt_rn(acc) : 0.0f;
             pt[j] = make_float4(s_unorm[u8_of(px[j], 0)], s_unorm[u8_of(px[j], 1)], s_unorm[u8_of(px[j], 2)], w);
@@ -260,9 +291,10 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
     // RangeFit::new (range.rs:44-101): the first point starts both ends; a later
     // point moves start on a strictly smaller dot, else end on a strictly larger one
     float s0 = 0.0f, s1 = 0.0f, s2 = 0.0f, e0 = 0.0f, e1 = 0.0f, e2 = 0.0f;
-    {
+    if (count > 0) {
         bool seen = false;
         float mn = 0.0f, mx = 0.0f;
+        int si = 0, ei = 0;
 #pragma unroll 4
         for (int i = 0; i < 16; ++i) {
             const float4 q = pt[i];
@@ -271,10 +303,13 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
             const bool first = p && !seen;
             const bool lo = first || (p && d < mn);
             const bool hi = first || (p && !(d < mn) && d > mx);
-            s0 = lo ? q.x : s0; s1 = lo ? q.y : s1; s2 = lo ? q.z : s2; mn = lo ? d : mn;
-            e0 = hi ? q.x : e0; e1 = hi ? q.y : e1; e2 = hi ? q.z : e2; mx = hi ? d : mx;
+            si = lo ? i : si; mn = lo ? d : mn;
+            ei = hi ? i : ei; mx = hi ? d : mx;
             seen = seen || p;
         }
+        const float4 qs = pt[si], qe = pt[ei];
+        s0 = qs.x; s1 = qs.y; s2 = qs.z;
+        e0 = qe.x; e1 = qe.y; e2 = qe.z;
     }
     s0 = snap(s0, 31.0f, 1.0f / 31.0f); s1 = snap(s1, 63.0f, 1.0f / 63.0f); s2 = snap(s2, 31.0f, 1.0f / 31.0f);
     e0 = snap(e0, 31.0f, 1.0f / 31.0f); e1 = snap(e1, 63.0f, 1.0f / 63.0f); e2 = snap(e2, 31.0f, 1.0f / 31.0f);
@@ -286,34 +321,58 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
     // compression_helper (range.rs:103-143) over a codebook of nc codes.  The
     // error sum adds +0 for pixels that are not points (it starts at +0 and
     // its terms are non-negative).
+    // The weighted differences w (x - c) of codes (0,1) and (2,3) are formed
+    // in pairs by the paired f32 operations add2_rn / mul2_rn (each lane the
+    // IEEE operation of the scalar form, x - c being x + (-c); an add followed
+    // by a multiply leaves nothing to fuse).  The squares and their sum stay
+    // scalar: a paired multiply followed by a paired add was contracted into
+    // a fused multiply-add even when written with .rn, which changes the
+    // rounding.  So every distance is the reference's
+    // ((w0 (x - cr))^2 + (w1 (y - cg))^2) + (w2 (z - cb))^2.
+    const float2 W0 = make_float2(w0, w0), W1 = make_float2(w1, w1), W2 = make_float2(w2, w2);
     auto helper = [&](const float (&cr)[4], const float (&cg)[4], const float (&cb)[4], int nc,
                       uint32_t &indices) -> bool {
+        const float2 nr01 = make_float2(-cr[0], -cr[1]), nr23 = make_float2(-cr[2], -cr[3]);
+        const float2 ng01 = make_float2(-cg[0], -cg[1]), ng23 = make_float2(-cg[2], -cg[3]);
+        const float2 nb01 = make_float2(-cb[0], -cb[1]), nb23 = make_float2(-cb[2], -cb[3]);
         uint32_t closest = 0;
         float err = 0.0f;
 #pragma unroll 4
         for (int i = 0; i < 16; ++i) {
             const float4 q = pt[i];
+            const float2 X = make_float2(q.x, q.x), Y = make_float2(q.y, q.y), Z = make_float2(q.z, q.z);
+            const float2 dx01 = mul2_rn(W0, add2_rn(X, nr01)), dx23 = mul2_rn(W0, add2_rn(X, nr23));
+            const float2 dy01 = mul2_rn(W1, add2_rn(Y, ng01)), dy23 = mul2_rn(W1, add2_rn(Y, ng23));
+            const float2 dz01 = mul2_rn(W2, add2_rn(Z, nb01)), dz23 = mul2_rn(W2, add2_rn(Z, nb23));
+            const float dx[4] = {dx01.x, dx01.y, dx23.x, dx23.y}, dy[4] = {dy01.x, dy01.y, dy23.x, dy23.y};
+            const float dz[4] = {dz01.x, dz01.y, dz23.x, dz23.y};
+            float d[4];
+#pragma unroll
+            for (int j = 0; j < 4; ++j) d[j] = dx[j] * dx[j] + dy[j] * dy[j] + dz[j] * dz[j];
             float dist = FLT_MAX;
             uint32_t idx = 0;
 #pragma unroll
             for (int j = 0; j < 4; ++j) {
                 if (j < nc) {
-                    const float dx = w0 * (q.x - cr[j]), dy = w1 * (q.y - cg[j]), dz = w2 * (q.z - cb[j]);
-                    const float d = dx * dx + dy * dy + dz * dz;
-                    idx = d < dist ? (uint32_t)j : idx;
-                    dist = d < dist ? d : dist;
+                    idx = d[j] < dist ? (uint32_t)j : idx;
+                    dist = d[j] < dist ? d[j] : dist;
                 }
             }
             closest |= idx << (2 * i);
             err = err + (((newbits >> i) & 1u) ? dist : 0.0f);
         }
         if (err < best_err) {
-            uint32_t out = 0;
+            // remap_indices (colourset.rs:130-141); with 16 distinct valid
+            // pixels every pixel is its own point and the map is the identity
+            uint32_t out = closest;
+            if (newbits != 0xFFFFu) {
+                out = 0;
 #pragma unroll
-            for (int p = 0; p < 16; ++p) {
-                const uint32_t r = (uint32_t)((repn >> (4 * p)) & 0xFu);
-                const uint32_t v = ((valid >> p) & 1u) ? ((closest >> (2 * r)) & 3u) : 3u;
-                out |= v << (2 * p);
+                for (int p = 0; p < 16; ++p) {
+                    const uint32_t r = dd_rep(dd, p);
+                    const uint32_t v = ((valid >> p) & 1u) ? ((closest >> (2 * r)) & 3u) : 3u;
+                    out |= v << (2 * p);
+                }
             }
             indices = out;
             best_err = err;

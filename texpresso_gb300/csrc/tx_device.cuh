@@ -94,6 +94,34 @@ __host__ __device__ constexpr int block_bytes(int fmt) { return (fmt == BC1 || f
 // exact scalar helpers (lib/src/math.rs:100-102, lib/src/math/vec4.rs:94-110)
 
 __device__ __forceinline__ float rcp_rn(float x) { return __frcp_rn(x); }   // == 1.0f / x
+
+// Paired f32 operations (sm_100+): each lane is the IEEE round-to-nearest
+// operation of the scalar form.  A paired multiply whose result feeds a
+// paired add can still end up fused into one multiply-add (measured: the
+// rounding of a squared-distance sum changed), so use them only where no
+// multiply feeds an add.
+__device__ __forceinline__ float2 add2_rn(float2 a, float2 b) {
+    float2 d;
+    asm("{.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "add.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
+__device__ __forceinline__ float2 mul2_rn(float2 a, float2 b) {
+    float2 d;
+    asm("{.reg .b64 ra, rb, rd;\n\t"
+        "mov.b64 ra, {%2, %3};\n\t"
+        "mov.b64 rb, {%4, %5};\n\t"
+        "mul.rn.f32x2 rd, ra, rb;\n\t"
+        "mov.b64 {%0, %1}, rd;}"
+        : "=f"(d.x), "=f"(d.y)
+        : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+    return d;
+}
 __device__ __forceinline__ float div_rn(float a, float b) { return __fdiv_rn(a, b); }
 __device__ __forceinline__ float sqrt_rn(float x) { return __fsqrt_rn(x); }
 
@@ -398,10 +426,12 @@ __device__ __forceinline__ uint2 write_alpha_block(uint32_t a0, uint32_t a1, con
 }
 
 // compress_bc3 for one channel: v = 16 packed values, mask = valid pixels.
-__device__ __forceinline__ uint2 encode_bc3_alpha(const uint32_t (&v)[4], uint32_t mask) {
+// FULL: every pixel is valid (mask == 0xFFFF), so the byte masks fold away.
+template <bool FULL>
+__device__ __forceinline__ uint2 encode_bc3_alpha_t(const uint32_t (&v)[4], uint32_t mask) {
     uint32_t vm[4];
 #pragma unroll
-    for (int r = 0; r < 4; ++r) vm[r] = nibble_to_bytemask((mask >> (4 * r)) & 0xFu);
+    for (int r = 0; r < 4; ++r) vm[r] = FULL ? 0xFFFFFFFFu : nibble_to_bytemask((mask >> (4 * r)) & 0xFu);
     // Ranges (alpha.rs:194-212).  Masked pixels enter as 255 for the minima and
     // 0 for the maxima (the initial values).  min5 skips zeros: the minimum of
     // (x - 1) mod 256 plus one, where a zero becomes 255 and a masked pixel
@@ -466,6 +496,12 @@ __device__ __forceinline__ uint2 encode_bc3_alpha(const uint32_t (&v)[4], uint32
         return write_alpha_block((uint32_t)max7, (uint32_t)min7, out);
     }
     return write_alpha_block((uint32_t)min7, (uint32_t)max7, i7);
+}
+
+// Interior blocks (all 16 pixels valid, the common case) take the form
+// without per-pixel masks; the bytes are the same either way.
+__device__ __forceinline__ uint2 encode_bc3_alpha(const uint32_t (&v)[4], uint32_t mask) {
+    return mask == 0xFFFFu ? encode_bc3_alpha_t<true>(v, mask) : encode_bc3_alpha_t<false>(v, mask);
 }
 
 // Gather one byte channel of 16 RGBA8 pixels into 4 packed words.

@@ -518,6 +518,7 @@ int tx_server_create(const tx_server_config *config, tx_server **out) {
             t.team_threads_per_cta = u.team_threads_per_cta;
         if (u.team_ctas_per_sm >= 1 && u.team_ctas_per_sm <= 16) t.team_ctas_per_sm = u.team_ctas_per_sm;
         if (u.team_blocks_per_unit >= 1 && u.team_blocks_per_unit <= 64) t.team_blocks_per_unit = u.team_blocks_per_unit;
+        if (u.team_blocks_in_flight >= 1 && u.team_blocks_in_flight <= 3) t.team_blocks_in_flight = u.team_blocks_in_flight;
         if (u.lane_ctas_per_sm >= 1 && u.lane_ctas_per_sm <= 16) t.lane_ctas_per_sm = u.lane_ctas_per_sm;
         if (u.lane_blocks_per_lane >= 1 && u.lane_blocks_per_lane <= 64) t.lane_blocks_per_lane = u.lane_blocks_per_lane;
         cfg.tuning = t;
