@@ -524,7 +524,7 @@ def run_ours(args):
         "clocks": clk,
     }
 
-    summary = {}
+    summary, non_ties = {}, 0
     if rank == 0 and world_size == 1:
         from oracle import oracle
         cores = oracle.online_cores()
@@ -537,31 +537,33 @@ def run_ours(args):
         par = oracle_parity(oracle, 2, img, 1, tx.COLOUR_WEIGHTS_PERCEPTUAL, False,
                             run.outputs(max(args.steps, args.warmup)) + [e2e_out])
         line["parity"] = par
-        summary["C1 BC3 ClusterFit (headline)"] = {
-            "mblocks_s": round(value, 1), "e2e": round(e2e_value, 1), "cpu": round(cpu_v, 3),
-            "issue_frac": roofline.get("frac"), "identical": par["identical_fraction"], "ties": par["ties"],
-            "non_ties": par["non_ties"]}
+        non_ties += par["non_ties"]
+        summary["cols"] = ["Mblocks/s", "cpu Mblocks/s", "hbm frac", "issue frac", "identical frac", "ties",
+                           "non-ties"]
+        summary["c1_bc3_cluster (headline)"] = [round(value, 1), round(cpu_v, 3), line["roofline_hbm"]["frac"],
+                                                roofline.get("frac"), par["identical_fraction"], par["ties"],
+                                                par["non_ties"]]
         if not args.no_extra:
             line["extra"] = extras(torch, tx, oracle, args, hbm_peak, fp32_peak_tops, ctr, sm_max_mhz)
-            for label, rec in line["extra"].items():
-                summary[label] = {k: v for k, v in (
-                    ("mblocks_s", round(rec["mblocks_s"], 1)), ("cpu", rec.get("cpu_mblocks_s")),
-                    ("hbm_frac", rec["hbm"]["frac"]), ("issue_frac", (rec.get("issue") or {}).get("frac")),
-                    ("identical", rec["parity"]["identical_fraction"]), ("ties", rec["parity"]["ties"]),
-                    ("non_ties", rec["parity"]["non_ties"])) if v is not None}
+            for key, rec in zip(CASES, line["extra"].values()):
+                pr = rec["parity"]
+                non_ties += pr["non_ties"]
+                summary[key] = [round(rec["mblocks_s"], 1), rec.get("cpu_mblocks_s"), rec["hbm"]["frac"],
+                                (rec.get("issue") or {}).get("frac"), pr["identical_fraction"], pr["ties"],
+                                pr["non_ties"]]
             line["batched"] = batched(torch, tx, args)
-            summary["C3 batched"] = {k: line["batched"][k] for k in (
-                "batch_mblocks_s", "gain_vs_per_call_eager", "gain_vs_per_call_graph", "identical_to_per_call")}
-            summary["C3 batched"]["tuning"] = line["batched"]["tuning"]
+            bt = line["batched"]
+            summary["c3 batched"] = {"Mblocks/s": bt["batch_mblocks_s"], "gain_eager": bt["gain_vs_per_call_eager"],
+                                     "gain_graph": bt["gain_vs_per_call_graph"], "same": bt["identical_to_per_call"],
+                                     "tuning": list(bt["tuning"].values())}
             line["serving"] = serving(torch, tx, args)
-            summary["C4 serving (served, plain)"] = {
-                r: {"gain": v["throughput_gain"], "req_s": [v["served"]["throughput_req_s"],
-                                                           v["plain"]["throughput_req_s"]],
-                    "p50": [v["served"]["p50_ms"], v["plain"]["p50_ms"]],
-                    "p99": [v["served"]["p99_ms"], v["plain"]["p99_ms"]],
-                    "busy": [v["served"]["busy_frac"], v["plain"]["busy_frac"]], "same": v["identical_outputs"]}
-                for r, v in line["serving"]["rates"].items()}
-    non_ties = sum(v.get("non_ties", 0) for v in summary.values() if isinstance(v, dict))
+            sv = {"cols": ["gain", "req/s served", "req/s plain", "p50 served", "p50 plain", "p99 served",
+                           "p99 plain", "busy served", "busy plain", "same"]}
+            for r, v in line["serving"]["rates"].items():
+                sv[r] = [v["throughput_gain"], v["served"]["throughput_req_s"], v["plain"]["throughput_req_s"],
+                         v["served"]["p50_ms"], v["plain"]["p50_ms"], v["served"]["p99_ms"], v["plain"]["p99_ms"],
+                         v["served"]["busy_frac"], v["plain"]["busy_frac"], v["identical_outputs"]]
+            summary["c4 serving"] = sv
     if summary:
         # last key of the line, so that a reader of the line's tail sees every case
         line["summary"] = summary

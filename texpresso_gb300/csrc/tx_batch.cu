@@ -45,7 +45,7 @@ cudaError_t upload_batch_tables(const uint32_t lut[4][256][2]) {
     return e;
 }
 
-__global__ void __launch_bounds__(128) k_batch_lanes(BatchQueue q) {
+__global__ void __launch_bounds__(128, 5) k_batch_lanes(BatchQueue q) {
     __shared__ float s_unorm[256];
     __shared__ float s_sqrt[17];
     __shared__ float4 s_pts[16 * 128];

@@ -8,7 +8,7 @@
 namespace tx {
 
 template <int FMT>
-__global__ void __launch_bounds__(128) k_range(SrcDesc src, DevParams prm, uint8_t *__restrict__ out,
+__global__ void __launch_bounds__(128, 6) k_range(SrcDesc src, DevParams prm, uint8_t *__restrict__ out,
                                                size_t nblocks) {
     __shared__ float s_unorm[256];
     __shared__ float s_sqrt[17];

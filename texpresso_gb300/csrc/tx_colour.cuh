@@ -172,25 +172,25 @@ struct PointCol {
 // for points only).  Keys: the RGB of a valid pixel, or 0x01000000 | p for a
 // pixel that is not (so it matches nothing).
 __device__ __forceinline__ void colour_dedup(const uint32_t (&key)[16], uint32_t (&res)[4]) {
-    uint64_t repn = 0, dupc = 0;  // nibble p: point index of pixel p / later pixels joining point p
+    // One comparison per pair j < i: it moves i's point down to j (the last
+    // assignment, at the smallest j, wins) and counts i as a later pixel of
+    // j's colour in the high nibble of byte j.  Every shift is a constant.
+    uint32_t cnt[4] = {0u, 0u, 0u, 0u};
+#pragma unroll
+    for (int w = 0; w < 4; ++w) res[w] = 0u;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-        int r = i;
+        uint32_t r = (uint32_t)i;
 #pragma unroll
-        for (int j = i - 1; j >= 0; --j) r = (key[j] == key[i]) ? j : r;
-        repn |= (uint64_t)r << (4 * i);
-        if (r != i) dupc += 1ull << (4 * r);
-    }
-#pragma unroll
-    for (int w = 0; w < 4; ++w) {
-        uint32_t x = 0;
-#pragma unroll
-        for (int c = 0; c < 4; ++c) {
-            const int i = 4 * w + c;
-            x |= (uint32_t)(((repn >> (4 * i)) & 0xFu) | (((dupc >> (4 * i)) & 0xFu) << 4)) << (8 * c);
+        for (int j = i - 1; j >= 0; --j) {
+            const bool e = key[j] == key[i];
+            r = e ? (uint32_t)j : r;
+            cnt[j >> 2] += e ? (0x10u << (8 * (j & 3))) : 0u;
         }
-        res[w] = x;
+        res[i >> 2] |= r << (8 * (i & 3));
     }
+#pragma unroll
+    for (int w = 0; w < 4; ++w) res[w] |= cnt[w];
 }
 
 // Point index and (pixel count - 1) of pixel i from colour_dedup's bytes.
@@ -199,8 +199,11 @@ __device__ __forceinline__ uint32_t dd_dup(const uint32_t (&res)[4], int i) {
     return (res[i >> 2] >> (8 * (i & 3) + 4)) & 0xFu;
 }
 
+// px is overwritten with the colour-set keys (the RGB bytes of every valid
+// pixel are kept; alpha is not needed after the packed copy below), so the
+// pixels and the keys never occupy registers at the same time.
 template <int FMT>
-__device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], uint32_t inb,
+__device__ __forceinline__ uint2 colour_range_thread(uint32_t (&px)[16], uint32_t inb,
                                                      const DevParams &prm, const float *s_unorm,
                                                      const float *s_sqrt, const PointCol &pt) {
     // ColourSet (colourset.rs:35-112), pixel-indexed: a "point" is the first
@@ -213,13 +216,12 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
     }
     const uint32_t valid = inb & ~tbits;
     const bool transparent = tbits != 0;
-    uint32_t dd[4];  // byte p: pixel p's point index | (its colour's pixel count - 1) << 4
-    {
-        uint32_t key[16];
+    uint32_t a4[4];  // alpha of pixel 4r + c at byte c of a4[r] (alpha weighting only)
+    if (prm.alpha_weighted) channel_words(px, 3, a4);
 #pragma unroll
-        for (int i = 0; i < 16; ++i) key[i] = ((valid >> i) & 1u) ? (px[i] & 0xFFFFFFu) : (0x01000000u | (uint32_t)i);
-        colour_dedup(key, dd);
-    }
+    for (int i = 0; i < 16; ++i) px[i] = ((valid >> i) & 1u) ? (px[i] & 0xFFFFFFu) : (0x01000000u | (uint32_t)i);
+    uint32_t dd[4];  // byte p: pixel p's point index | (its colour's pixel count - 1) << 4
+    colour_dedup(px, dd);
     // a valid pixel that is its own point starts a new point (excluded pixels
     // match nothing, so they are their own "point" too and are masked out)
     uint32_t newbits = 0;
@@ -234,7 +236,7 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
     if (count == 1) {
         uint32_t rgb = 0;
 #pragma unroll
-        for (int i = 0; i < 16; ++i) rgb |= ((valid >> i) & 1u) ? (px[i] & 0xFFFFFFu) : 0u;
+        for (int i = 0; i < 16; ++i) rgb |= ((valid >> i) & 1u) ? px[i] : 0u;
         int col[3];
 #pragma unroll
         for (int c = 0; c < 3; ++c) col[c] = f32_to_i32_clamped(s_unorm[u8_of(rgb, c)] * 255.0f, 255);
@@ -259,7 +261,7 @@ __device__ __forceinline__ uint2 colour_range_thread(const uint32_t (&px)[16], u
             float acc = 0.0f;
 #pragma unroll
             for (int i = j; i < 16; ++i) {
-                const float wa = (float)((px[i] >> 24) + 1u) * (1.0f / 256.0f);
+                const float wa = (float)(((a4[i >> 2] >> (8 * (i & 3))) & 0xFFu) + 1u) * (1.0f / 256.0f);
                 acc = acc + ((((valid >> i) & 1u) && (int)dd_rep(dd, i) == j) ? wa : 0.0f);
             }
             const float w = ((newbits >> j) & 1u) ? sqrt_rn(acc) : 0.0f;
