@@ -256,17 +256,24 @@ __device__ __forceinline__ uint2 colour_range_thread(uint32_t (&px)[16], uint32_
             pt[i] = make_float4(s_unorm[u8_of(px[i], 0)], s_unorm[u8_of(px[i], 1)], s_unorm[u8_of(px[i], 2)], w);
         }
     } else {
+        // alpha weights (colourset.rs:69-74, :94-97): every valid pixel adds
+        // (a + 1) / 256 to its point's weight in pixel order, the point's own
+        // pixel first (0 + w = w); an excluded pixel adds +0 to its own slot,
+        // which stays +0.  Then sqrt for the points.
 #pragma unroll
-        for (int j = 0; j < 16; ++j) {
-            float acc = 0.0f;
+        for (int j = 0; j < 16; ++j)
+            pt[j] = make_float4(s_unorm[u8_of(px[j], 0)], s_unorm[u8_of(px[j], 1)], s_unorm[u8_of(px[j], 2)], 0.0f);
 #pragma unroll
-            for (int i = j; i < 16; ++i) {
-                const float wa = (float)(((a4[i >> 2] >> (8 * (i & 3))) & 0xFFu) + 1u) * (1.0f / 256.0f);
-                acc = acc + ((((valid >> i) & 1u) && (int)dd_rep(dd, i) == j) ? wa : 0.0f);
-            }
-            const float w = ((newbits >> j) & 1u) ? sqrt_rn(acc) : 0.0f;
-            pt[j] = make_float4(s_unorm[u8_of(px[j], 0)], s_unorm[u8_of(px[j], 1)], s_unorm[u8_of(px[j], 2)], w);
+        for (int i = 0; i < 16; ++i) {
+            const float wa = ((valid >> i) & 1u)
+                                 ? (float)(((a4[i >> 2] >> (8 * (i & 3))) & 0xFFu) + 1u) * (1.0f / 256.0f)
+                                 : 0.0f;
+            float &w = pt[(int)dd_rep(dd, i)].w;
+            w = w + wa;
         }
+#pragma unroll
+        for (int j = 0; j < 16; ++j)
+            if ((newbits >> j) & 1u) pt[j].w = sqrt_rn(pt[j].w);
     }
 
     // Sym3x3::weighted_covariance (math.rs:44-73)
