@@ -579,7 +579,7 @@ def run_ours(args):
 
 
 CASES = ["c0_bc1_cluster", "c1_bc3_range", "c1_bc3_cluster_aw", "c1_bc3_range_aw", "bc1_iter_cluster",
-         "c2_bc4_r8", "c2_bc5_rg8", "c2_bc4_rgba", "c2_bc5_rgba", "c1_bc3_cluster"]
+         "bc3_iter_cluster", "c2_bc4_r8", "c2_bc5_rg8", "c2_bc4_rgba", "c2_bc5_rgba", "c1_bc3_cluster"]
 
 
 def extra_cases(tx, names=None):
@@ -611,6 +611,7 @@ def extra_cases(tx, names=None):
         "c1_bc3_range_aw": ("C1 BC3 RangeFit alpha-weighted 2048x2048", 2, lambda: img("c1"),
                             P(algorithm=R, weigh_colour_by_alpha=True), 0, 4),
         "bc1_iter_cluster": ("BC1 IterativeClusterFit 2048x2048", 0, lambda: img("iter"), P(algorithm=I), 2, 4),
+        "bc3_iter_cluster": ("BC3 IterativeClusterFit 2048x2048", 2, lambda: img("c1"), P(algorithm=I), 2, 4),
         "c2_bc4_r8": ("C2 BC4 4096x4096 R8", 3, lambda: np.ascontiguousarray(img("noise")[..., :1]), P(), 1, 1),
         "c2_bc5_rg8": ("C2 BC5 4096x4096 RG8", 4, lambda: np.ascontiguousarray(img("noise")), P(), 1, 2),
         "c2_bc4_rgba": ("C2 BC4 4096x4096 RGBA8", 3, lambda: workloads.expand_to_rgba(img("noise")), P(), 1, 4),
