@@ -30,6 +30,7 @@ struct DeviceState {
     std::mutex mu;                      // serialises host-buffer calls on this device
     std::atomic<int> ready{0};          // tables uploaded
     cudaStream_t streams[kStreams] = {};
+    cudaEvent_t joined[kStreams] = {};  // streams 1.. joined into stream 0 at the end of a call
     uint8_t *d_in = nullptr;
     size_t in_cap = 0;
     uint8_t *d_out = nullptr;
@@ -120,8 +121,10 @@ int ensure_ready(DeviceState **out) {
     cudaError_t e = tx::upload_colour_tables(lut);
     if (e != cudaSuccess) return fail(e);
     if ((e = tx::upload_batch_tables(lut)) != cudaSuccess) return fail(e);
-    for (int s = 0; s < kStreams; ++s)
+    for (int s = 0; s < kStreams; ++s) {
         if ((e = cudaStreamCreateWithFlags(&d.streams[s], cudaStreamNonBlocking)) != cudaSuccess) return fail(e);
+        if ((e = cudaEventCreateWithFlags(&d.joined[s], cudaEventDisableTiming)) != cudaSuccess) return fail(e);
+    }
     if ((e = cudaDeviceGetAttribute(&d.sm_count, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess) return fail(e);
     d.ready.store(1, std::memory_order_release);
     return TX_OK;
@@ -259,12 +262,27 @@ int tx_compress(int format, const uint8_t *rgba, size_t rgba_len, size_t width, 
     const size_t bs = tx_block_size(format), bw = tx_num_blocks(width);
     const size_t rows = (nblocks + bw - 1) / bw;  // output block rows (may exceed the image)
     const size_t pitch = 4 * width;
-    size_t nbands = rows / 32;
+    // Bands of block rows, each copied in, compressed and copied out on one of
+    // the streams, so the copies of one band overlap the kernels of others.
+    // Large images taper the bands (weights 1 4 8 8 8 8 8 4 1 of 50): the
+    // first band's upload and the last band's download are the only copies
+    // nothing overlaps, so they are kept small.
+    static const int kTaper[] = {1, 4, 8, 8, 8, 8, 8, 4, 1};
+    constexpr int kTaperBands = 9, kTaperSum = 50;
+    const bool taper = rows >= 2 * kTaperSum;
+    size_t nbands = taper ? kTaperBands : rows / 32;
     if (nbands < 1) nbands = 1;
-    if (nbands > 8) nbands = 8;
+    if (nbands > 8 && !taper) nbands = 8;
     const size_t band_rows = (rows + nbands - 1) / nbands;
-    for (size_t r0 = 0, band = 0; r0 < rows; r0 += band_rows, ++band) {
-        const size_t r1 = r0 + band_rows < rows ? r0 + band_rows : rows;
+    size_t done_w = 0;
+    for (size_t r0 = 0, band = 0; r0 < rows; ++band) {
+        size_t r1;
+        if (taper) {
+            done_w += (size_t)kTaper[band];
+            r1 = band + 1 == (size_t)kTaperBands ? rows : rows * done_w / kTaperSum;
+        } else {
+            r1 = r0 + band_rows < rows ? r0 + band_rows : rows;
+        }
         cudaStream_t st = d->streams[band % kStreams];
         // input rows of this band
         const size_t y0 = 4 * r0, y1 = (4 * r1 < height) ? 4 * r1 : height;
@@ -288,9 +306,14 @@ int tx_compress(int format, const uint8_t *rgba, size_t rgba_len, size_t width, 
         if ((e = cudaMemcpyAsync(output + b0 * bs, d->d_out + b0 * bs, (b1 - b0) * bs, cudaMemcpyDeviceToHost, st)) !=
             cudaSuccess)
             return fail(e);
+        r0 = r1;
     }
-    for (int s = 0; s < kStreams; ++s)
-        if ((e = cudaStreamSynchronize(d->streams[s])) != cudaSuccess) return fail(e);
+    // one wait: the other streams join stream 0
+    for (int s = 1; s < kStreams; ++s) {
+        if ((e = cudaEventRecord(d->joined[s], d->streams[s])) != cudaSuccess) return fail(e);
+        if ((e = cudaStreamWaitEvent(d->streams[0], d->joined[s], 0)) != cudaSuccess) return fail(e);
+    }
+    if ((e = cudaStreamSynchronize(d->streams[0])) != cudaSuccess) return fail(e);
     return TX_OK;
 }
 
