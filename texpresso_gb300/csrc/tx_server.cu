@@ -99,6 +99,7 @@ struct tx_server {
     size_t held = 0, held_high = 0;  // bytes held by admitted requests (worker only; stats under mu)
     double busy_us = 0;              // compression-step time on the device (worker only; stats under mu)
     uint64_t hbm_waits = 0;          // admissions deferred for lack of free device memory
+    double hbm_retry_at = 0;         // worker only: earliest time to query free memory again
     cudaStream_t s_load = nullptr, s_comp = nullptr, s_store = nullptr;
     Step steps[2];
     uint32_t max_items = 0, max_units = 0;
@@ -195,10 +196,14 @@ int admit(tx_server *s) {
         if (s->held + q->footprint > s->cfg.memory_budget) break;
         cudaError_t e;
         if (!queried || avail < q->footprint) {
+            // while the head waits for memory that another process holds, ask
+            // the driver at most every 200 us (a completion of ours resets it)
+            if (q->hbm_deferred && now_us() < s->hbm_retry_at) break;
             if ((e = hbm_available(s, &avail)) != cudaSuccess) return fail_server(e);
             queried = true;
         }
         if (avail < q->footprint) {
+            s->hbm_retry_at = now_us() + 200.0;
             if (!q->hbm_deferred) {
                 q->hbm_deferred = true;
                 std::lock_guard<std::mutex> lk(s->mu);
@@ -389,6 +394,7 @@ int progress(tx_server *s, bool *completed_any) {
                 // back to the pool behind the copies (done_ev has completed)
                 if ((e = cudaFreeAsync(q->dev, s->s_store)) != cudaSuccess) return fail_server(e);
                 q->dev = nullptr;
+                s->hbm_retry_at = 0;  // memory came back: a waiting head may fit now
                 std::lock_guard<std::mutex> lk(s->mu);
                 s->held -= q->footprint;
                 q->t_done = now_us();
