@@ -46,8 +46,10 @@ __global__ void __launch_bounds__(256, 4) k_cluster(SrcDesc src, DevParams prm, 
     // blocks one at a time from a shared counter, so a team that drew cheap
     // blocks (one colour, one ordering) takes more of them instead of idling
     // until the CTA's slowest team is done, and teams working at the same time
-    // still read neighbouring pixels.  The next block's pixels are requested
-    // before the current block is encoded.
+    // still read neighbouring pixels.  For BC2/BC3 the next block's pixels are
+    // requested before the current block is encoded; BC1, whose compress3 +
+    // compress4 code already runs at the register limit, measured faster
+    // without that (163 vs 159 Mblocks/s; BC3: 254 vs 265).
     auto take = [&]() {
         uint32_t k = 0;
         if (tm.lane == 0) k = atomicAdd(&s_next, 1u);
@@ -55,6 +57,11 @@ __global__ void __launch_bounds__(256, 4) k_cluster(SrcDesc src, DevParams prm, 
         return ((size_t)(k >> 3) * gridDim.x + blockIdx.x) * 8u + (k & 7u);
     };
     const size_t end_chunk = (nblocks + 7) / 8 * 8;  // slots past this belong to no chunk
+    if (FMT == BC1) {
+        for (size_t b = take(); b < end_chunk; b = take())
+            if (b < nblocks) cluster_block_px<FMT, TEAM, NITER>(tm, sm, tt, load_team_pixel(src, b, tm.lane), b, prm, out);
+        return;
+    }
     size_t b = take();
     TeamPixel tp{0u, false};
     if (b < nblocks) tp = load_team_pixel(src, b, tm.lane);
@@ -90,9 +97,10 @@ template <int FMT, int TEAM, int NITER>
 static cudaError_t launch_cluster_t(const SrcDesc &src, const DevParams &prm, uint8_t *out, size_t nblocks,
                                     cudaStream_t st, const LaunchCfg &cfg) {
     // A launch smaller than one wave of 8-team CTAs (SMs x 4 x 8 blocks) runs
-    // in 4-team CTAs: twice as many CTAs spread more evenly over the SMs (for
-    // 4,096 blocks, at most 7 CTAs on an SM against 6.7 on average, instead
-    // of 4 against 3.4), and the slowest SM sets the launch's time.
+    // in 2-team CTAs: four times as many CTAs spread more evenly over the SMs
+    // (for 4,096 blocks, 13-14 CTAs on an SM against 13.5 on average, instead
+    // of 4 against 3.4), and the slowest SM sets the launch's time.  (4-team
+    // CTAs: 28.0 us for the 256x256 BC1 launch, 2-team 27.5 us, 1-team 29.3.)
     static int sm_count[64] = {};
     int dev0 = 0;
     cudaGetDevice(&dev0);
@@ -104,7 +112,7 @@ static cudaError_t launch_cluster_t(const SrcDesc &src, const DevParams &prm, ui
     int threads = cfg.cluster_threads;
     if (NITER == 1 && threads == 256 && dev0 < 64 && sm_count[dev0] > 0 &&
         nblocks < (size_t)sm_count[dev0] * 4 * (256 / TEAM))
-        threads = 128;
+        threads = 2 * TEAM;
     const size_t smem = cluster_smem_bytes(TEAM, threads);
     static bool attr_set[64] = {};
     int dev = 0;
