@@ -24,13 +24,20 @@ template <int FMT, int TEAM, int NITER>
 __global__ void __launch_bounds__(256, 4) k_cluster(SrcDesc src, DevParams prm, uint8_t *__restrict__ out,
                                                  size_t nblocks) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
+    // The u8 -> [0,1] and sqrt(count) tables: a ClusterFit CTA (8 blocks, then
+    // the next CTA) reads them from global memory through L1, because building
+    // them in shared memory cost each CTA 256 divisions and a barrier (BC3
+    // 2048x2048: 742 vs 776 us); the persistent IterativeClusterFit CTAs build
+    // them once and read shared memory (991 vs 999 us).
     __shared__ float s_unorm[256];
     __shared__ float s_sqrt[17];
     __shared__ uint32_t s_next;
-    if (threadIdx.x == 0) s_next = 0;
-    init_unorm_tables(s_unorm, s_sqrt);  // ends with __syncthreads
+    if (NITER > 1) {
+        if (threadIdx.x == 0) s_next = 0;
+        init_unorm_tables(s_unorm, s_sqrt);  // ends with __syncthreads
+    }
     TeamSmem *teams = reinterpret_cast<TeamSmem *>(smem_raw);
-    const TeamTables tt{g_cand, g_cand + kCand4 + 1, s_unorm, s_sqrt};
+    const TeamTables tt{g_cand, g_cand + kCand4 + 1, NITER > 1 ? s_unorm : g_unorm8, NITER > 1 ? s_sqrt : g_sqrt_count};
     const Team<TEAM> tm;
     TeamSmem &sm = teams[threadIdx.x / TEAM];
     if (NITER == 1) {

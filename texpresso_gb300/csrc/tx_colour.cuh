@@ -52,6 +52,10 @@ static __device__ uint32_t g_cand16[kCand4 + 1 + kCand3 + 1];
 // bits i | S(i,j) << 8 | S(j,k) << 16 (table offsets, one byte each).
 static __device__ float4 g_ub4[kCand4 + 1];
 static __device__ float4 g_ub3[kCand3 + 1];
+// unorm8(v) for every byte v and sqrt(n) for n <= 16 (filled by k_unorm_tables
+// with the same correctly rounded division and square root as the kernels).
+static __device__ float g_unorm8[256];
+static __device__ float g_sqrt_count[17];
 
 // Partial-sum table S(a,b), 0 <= a <= b <= 16, stored as the upper triangle
 // row by row: S(a,b) at tri_idx(a,b) (153 entries).
@@ -413,6 +417,12 @@ __device__ __forceinline__ void init_unorm_tables(float *s_unorm, float *s_sqrt)
     for (int i = threadIdx.x; i < 256; i += blockDim.x) s_unorm[i] = unorm8((uint32_t)i);
     if (threadIdx.x < 17) s_sqrt[threadIdx.x] = sqrt_rn((float)threadIdx.x);
     __syncthreads();
+}
+
+// The same tables in global memory (one CTA of 256 threads).
+static __global__ void k_unorm_tables() {
+    g_unorm8[threadIdx.x] = unorm8(threadIdx.x);
+    if (threadIdx.x < 17) g_sqrt_count[threadIdx.x] = sqrt_rn((float)threadIdx.x);
 }
 
 // ===========================================================================
@@ -1363,6 +1373,8 @@ static inline cudaError_t upload_tables_this_tu(const uint32_t lut[4][256][2]) {
     if ((e = cudaMemcpyToSymbol(c_one4, one4, sizeof(one4))) != cudaSuccess) return e;
     if ((e = cudaMemcpyToSymbol(c_one3, one3, sizeof(one3))) != cudaSuccess) return e;
     k_unit_terms<<<(kCand4 + 255) / 256, 256>>>();
+    if ((e = cudaGetLastError()) != cudaSuccess) return e;
+    k_unorm_tables<<<1, 256>>>();
     if ((e = cudaGetLastError()) != cudaSuccess) return e;
     if ((e = cudaDeviceSynchronize()) != cudaSuccess) return e;
     return cudaMemcpyToSymbol(c_lut, lut, sizeof(uint32_t) * 4 * 256 * 2);
