@@ -438,7 +438,7 @@ def run_reference(args):
             "cpu_baseline": {"value": round(value, 4), "unit": UNIT, "cores": cores, "kind": "port",
                              "sample": sample},
             "e2e": {"value": round(value, 4), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
-            "note": "the reference is Rust and no cargo/rustc exists here or on the GPU box; its algorithm runs "
+            "note": "the reference is Rust and no Rust toolchain (cargo/rustc) is installed; its algorithm runs "
                     "as the C oracle (oracle/texpresso_oracle.c) on all host cores"}
     print(json.dumps(line), flush=True)
     return 0
