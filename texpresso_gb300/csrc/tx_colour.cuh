@@ -755,7 +755,13 @@ struct SharedOrder {
 
 // ClusterFit::compress3 / compress4 (cluster.rs:152-417) for one team.
 // best_err / best carry the ColourFit state across compress3 -> compress4.
-template <int NC, int TEAM, int NITER>
+// LEAN (BC1 IterativeClusterFit, whose two passes make the largest kernel and
+// whose top stall is instruction fetch) trades unrolling for code size: the
+// rank and partial-sum loops are unrolled 4 times instead of 16, and short
+// lists go through the survivor sweep instead of a sweep of their own
+// (1,557 vs 1,604 us for 2048x2048; the other kernels measured faster
+// without these changes).
+template <int NC, int TEAM, int NITER, bool LEAN = false>
 __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm, const uint32_t *tbl, int count,
                                              const float (&principal)[3], const float (&cw)[3], bool prune,
                                              bool valid, int my_point, bool unit16, float &best_err, uint2 &best,
@@ -787,10 +793,18 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
             if (lane < 16) {
                 // stable rank: entries with a smaller key, or an equal key earlier
                 int rank = 0;
+                if (LEAN) {
+#pragma unroll 4
+                    for (int f = 0; f < 16; ++f) {
+                        const uint32_t kf = sm.D[f];
+                        rank += (kf < ke || (kf == ke && f < lane)) ? 1 : 0;
+                    }
+                } else {
 #pragma unroll
-                for (int f = 0; f < 16; ++f) {
-                    const uint32_t kf = sm.D[f];
-                    rank += (kf < ke || (kf == ke && f < lane)) ? 1 : 0;
+                    for (int f = 0; f < 16; ++f) {
+                        const uint32_t kf = sm.D[f];
+                        rank += (kf < ke || (kf == ke && f < lane)) ? 1 : 0;
+                    }
                 }
                 reinterpret_cast<uint8_t *>(sm.hist[it])[rank] = (uint8_t)(lane < count ? lane : 0);
                 my_rank = rank;
@@ -815,13 +829,25 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
                 float4 acc = make_float4(0.f, 0.f, 0.f, 0.f);
                 float4 *row = sm.S + tri_idx(lane < 16 ? lane : 0, 0) + lane;  // &S(lane, lane)
                 if (lane < count) row[0] = acc;
+                if (LEAN) {
+#pragma unroll 4
+                    for (int s = 0; s < 16; ++s) {
+                        if (s >= count) break;
+                        if (lane + s < count) {
+                            const float4 q = sm.PW[lane + s];
+                            acc.x += q.x; acc.y += q.y; acc.z += q.z; acc.w += q.w;
+                            row[s + 1] = acc;
+                        }
+                    }
+                } else {
 #pragma unroll
-                for (int s = 0; s < 16; ++s) {
-                    if (s >= count) break;
-                    if (lane + s < count) {
-                        const float4 q = sm.PW[lane + s];
-                        acc.x += q.x; acc.y += q.y; acc.z += q.z; acc.w += q.w;
-                        row[s + 1] = acc;
+                    for (int s = 0; s < 16; ++s) {
+                        if (s >= count) break;
+                        if (lane + s < count) {
+                            const float4 q = sm.PW[lane + s];
+                            acc.x += q.x; acc.y += q.y; acc.z += q.z; acc.w += q.w;
+                            row[s + 1] = acc;
+                        }
                     }
                 }
             }
@@ -840,9 +866,17 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
         ob.ent = 0;
 #pragma unroll
         for (int c = 0; c < 3; ++c) { ob.a[c] = 0.0f; ob.b[c] = 0.0f; }
+        uint32_t lean_nq = 0;  // LEAN: candidates queued for the exact sweep below
         if (ncand <= 2u * TEAM || !prune) {
-            // short lists: the plain sweep, lane-strided over the candidates
-            for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) eval_candidate<NC>(sm, __ldg(tbl + t), xs, cw, ob);
+            if (LEAN) {
+                uint32_t *queue = reinterpret_cast<uint32_t *>(sm.LB);
+                for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) queue[t] = t;
+                lean_nq = ncand;
+                tm.sync();
+            } else {
+                // short lists: the plain sweep, lane-strided over the candidates
+                for (uint32_t t = (uint32_t)lane; t < ncand; t += TEAM) eval_candidate<NC>(sm, __ldg(tbl + t), xs, cw, ob);
+            }
         } else {
             // 1. a lower bound of every candidate's error (see cand_bound)
             const BoundBlock bb = bound_block(xs, cw);
@@ -928,7 +962,14 @@ __device__ __forceinline__ void cluster_pass(const Team<TEAM> &tm, TeamSmem &sm,
             }
             tm.sync();
             // 4. exact errors of the survivors
-            for (uint32_t s = (uint32_t)lane; s < nq; s += TEAM) eval_candidate<NC>(sm, __ldg(tbl + queue[s]), xs, cw, ob);
+            if (LEAN)
+                lean_nq = nq;
+            else
+                for (uint32_t s = (uint32_t)lane; s < nq; s += TEAM) eval_candidate<NC>(sm, __ldg(tbl + queue[s]), xs, cw, ob);
+        }
+        if (LEAN) {
+            const uint32_t *queue = reinterpret_cast<const uint32_t *>(sm.LB);
+            for (uint32_t s = (uint32_t)lane; s < lean_nq; s += TEAM) eval_candidate<NC>(sm, __ldg(tbl + queue[s]), xs, cw, ob);
         }
         // lexicographic reduction of the lanes' bests; the winning lane (the
         // one holding the winning entry) supplies the endpoints
@@ -1092,10 +1133,10 @@ __device__ __forceinline__ uint2 colour_cluster_team(const Team<TEAM> &tm, TeamS
                        cw[2] <= FLT_MAX;
     SharedOrder so{false, 0, false};
     if (FMT == BC1) {
-        cluster_pass<3, TEAM, NITER>(tm, sm, tbl3, count, principal, cw, prune, valid, my_point, unit16, best_err,
+        cluster_pass<3, TEAM, NITER, (NITER > 1)>(tm, sm, tbl3, count, principal, cw, prune, valid, my_point, unit16, best_err,
                                      best, so);
         if (!transparent)
-            cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, prune, valid, my_point, unit16, best_err,
+            cluster_pass<4, TEAM, NITER, (NITER > 1)>(tm, sm, tbl4, count, principal, cw, prune, valid, my_point, unit16, best_err,
                                          best, so);
     } else {
         cluster_pass<4, TEAM, NITER>(tm, sm, tbl4, count, principal, cw, prune, valid, my_point, unit16, best_err,
