@@ -104,10 +104,11 @@ template <int FMT, int TEAM, int NITER>
 static cudaError_t launch_cluster_t(const SrcDesc &src, const DevParams &prm, uint8_t *out, size_t nblocks,
                                     cudaStream_t st, const LaunchCfg &cfg) {
     // A launch smaller than one wave of 8-team CTAs (SMs x 4 x 8 blocks) runs
-    // in 2-team CTAs: four times as many CTAs spread more evenly over the SMs
-    // (for 4,096 blocks, 13-14 CTAs on an SM against 13.5 on average, instead
-    // of 4 against 3.4), and the slowest SM sets the launch's time.  (4-team
-    // CTAs: 28.0 us for the 256x256 BC1 launch, 2-team 27.5 us, 1-team 29.3.)
+    // in one-warp CTAs: they spread evenly over the SMs (for 4,096 blocks, 26-28
+    // on an SM against 3-4 CTAs of 8 teams), and a team that finishes frees
+    // its slot without waiting for CTA partners; the slowest SM sets the
+    // launch's time.  (256x256 BC1: 25.9 us in one-warp CTAs, 26.5 us in
+    // 2-team and 26.9 us in 4-team CTAs.)
     static int sm_count[64] = {};
     int dev0 = 0;
     cudaGetDevice(&dev0);
@@ -119,7 +120,7 @@ static cudaError_t launch_cluster_t(const SrcDesc &src, const DevParams &prm, ui
     int threads = cfg.cluster_threads;
     if (NITER == 1 && threads == 256 && dev0 < 64 && sm_count[dev0] > 0 &&
         nblocks < (size_t)sm_count[dev0] * 4 * (256 / TEAM))
-        threads = 2 * TEAM;
+        threads = 32;
     const size_t smem = cluster_smem_bytes(TEAM, threads);
     static bool attr_set[64] = {};
     int dev = 0;
